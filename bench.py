@@ -1,0 +1,352 @@
+"""Benchmark: FWI gradient throughput of the GB300 P/SV engine.
+
+Workload (the reference's FWI-iteration configuration): 301 x 601 grid,
+dx = dz = 0.5 m, 8 shots along a free surface, 120 receivers, 4th-order
+Holberg stencil, 20-cell CPML on three sides, dt = 5e-5 s, nt = 4000, FP32
+wavefields, snapshots every 3 steps (the reference's example setting,
+scripts/pre_proc_fwi.py:68).  Seeded synthetic layered-plus-anomaly model.
+
+One step = one FWI gradient over all 8 shots: forward with snapshot storage,
+residual and L2, time-reversed adjoint with the imaging condition, energy
+weights and scaling into the global gradients.
+metric = grid-point updates per second, forward + adjoint
+       = 8 shots * 2 passes * nt * nz * nx / step time.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt updates/s fwd+adj (FWI gradient)"
+UNIT = "updates/s"
+CFG = dict(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=8, fdorder=4, stencil="holberg",
+           npml=20, nrec=120, snap_dt=3)
+L2_BYTES = 129 * 2 ** 20
+
+
+def workload(nt=None, nshot=None):
+    from fwi_cuda_gb300 import survey as S
+    c = dict(CFG)
+    if nt is not None:
+        c["nt"] = nt
+    if nshot is not None:
+        c["nshot"] = nshot
+    sv, true, init = S.config_layered(nz=c["nz"], nx=c["nx"], dx=c["dx"], nt=c["nt"], dt=c["dt"],
+                                      nshot=c["nshot"], fdorder=c["fdorder"],
+                                      stencil=c["stencil"], npml=c["npml"], nrec=c["nrec"],
+                                      snap_dt=c["snap_dt"], seed=1234)
+    sv.imaging_sign = 1
+    return sv, true, init
+
+
+def config_dict(n_gpus, extra=None):
+    d = {"workload": "FWI gradient, 301x601 layered+anomaly, 8 shots, nt=4000, order-4 Holberg, "
+                     "free surface + 20-cell CPML, snap_dt=3",
+         "nz": CFG["nz"], "nx": CFG["nx"], "nt": CFG["nt"], "shots_per_gpu": CFG["nshot"],
+         "fdorder": CFG["fdorder"], "stencil": CFG["stencil"], "snap_dt": CFG["snap_dt"],
+         "precision": "fp32 wavefields, fp64 model/traces", "l2_flush": True,
+         "parallelism": f"shots sharded over {n_gpus} GPU(s), gradient all-reduce"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def updates_per_step(nt, nshot):
+    return 2.0 * nshot * nt * CFG["nz"] * CFG["nx"]
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(nt_sample=1000, threads=None):
+    """One shot, forward + adjoint gradient, cropped to nt_sample steps, on the
+    host cores: the reference's own code when oracle/_ref is built here, else
+    the oracle port (same loop structure and OpenMP placement)."""
+    from oracle import oracle as O
+    O.build()
+    kind = "reference" if O.ref_available() else "port"
+    lib = O.reference() if kind == "reference" else O.oracle()
+    cores = threads or os.cpu_count()
+    lib.set_threads(cores)
+    sv, true, init = workload(nt=nt_sample, nshot=1)
+    sv.stencil = "reference"  # the reference's stencil as written (2-point x hc[1])
+    lam, mu, rho = init
+    mz, rz, rx, _ = lib.mat_av2(lam, mu, rho)
+    t0 = time.perf_counter()
+    fwd = lib.kernel_PSV(sv, 0, lam, mu, mz, rz, rx, accu=True)
+    src = (sv.z_rec, sv.x_rec, np.zeros(sv.nrec, np.int32), 0)
+    lib.kernel_PSV(sv, 0, lam, mu, mz, rz, rx, grad=True, history=fwd["history"],
+                   stf=(fwd["rtf_uz"], fwd["rtf_ux"]), src=src, rec=False)
+    dt = time.perf_counter() - t0
+    upd = 2.0 * nt_sample * CFG["nz"] * CFG["nx"]
+    return dict(value=upd / dt, unit=UNIT, cores=cores, kind=kind,
+                sample=f"1 shot forward+adjoint gradient, 301x601, nt={nt_sample} "
+                       f"(of 4000), reference 2-point stencil at fdorder 4, FP64, {dt:.1f} s")
+
+
+# ----------------------------------------------------------------------------- clocks
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        load = [s for s in sm if smax and s > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- roofline
+def algorithmic_bytes(prof_kernel, snap_dt):
+    """Bytes per grid-point update each kernel must move (FP32) when every
+    field it touches crosses HBM exactly once: stress reads vz, vx (8 B),
+    reads and writes szz, szx, sxx (24 B), reads dt*lam, dt*(lam+2mu),
+    dt*mu_zx (12 B); velocity reads the 3 stresses (12 B), reads and writes
+    vz, vx (16 B), reads dt/rho_z, dt/rho_x (8 B), plus the energy (8 B),
+    displacement (16 B, adjoint) and the snapshot store or imaging terms
+    amortised over snap_dt."""
+    store = 20.0 / snap_dt           # 5 snapshot planes written every snap_dt steps
+    image = (20.0 + 24.0 + 8.0) / snap_dt  # history read + 3 gradients RW + 2 factors
+    return {"stress_fwd": 44.0, "stress_adj": 44.0,
+            "velocity_fwd": 36.0 + 8.0 + store,          # sigma R, v RW, 2 coef, We RW
+            "velocity_adj": 36.0 + 16.0 + 8.0 + image}[prof_kernel]  # + u RW, We_adj RW
+
+
+def read_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, rank, world):
+    import torch
+    from fwi_cuda_gb300 import _lib, engine
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    sv, true, init = workload()
+    nt, nshot = sv.nt, sv.nshot
+    with engine.Plan(sv, precision=32) as p:
+        p.set_model(*true)
+        obs_uz, obs_ux = p.forward()          # observed data from the true model
+        p.set_model(*init)
+        p.set_observed(obs_uz, obs_ux)
+        stream = torch.cuda.ExternalStream(p.stream)
+        flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+
+        def barrier():
+            if world > 1:
+                import torch.distributed as dist
+                dist.barrier()
+            torch.cuda.synchronize()
+
+        for _ in range(args.warmup):
+            p.gradient(fetch=False)
+        # ---- value: inputs resident, CUDA events on the plan's stream
+        barrier()
+        clk = Clocks(dev)
+        l0 = p.kernel_launches
+        times = []
+        for _ in range(args.steps):
+            flush.fill_(1.0)                    # evict L2 between steps
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            p.gradient(fetch=False)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        barrier()
+        clocks = clk.stop()
+        launches = p.kernel_launches - l0
+        ms = float(np.mean(times))
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        value = updates_per_step(nt, nshot) * world / (ms / 1e3)
+        split = p.timing()
+
+        # ---- e2e: through the C ABI with pinned host buffers each step
+        h_model = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() for a in init]
+        h_obs = [torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy() for a in (obs_uz, obs_ux)]
+        h_grad = [torch.empty((sv.nz, sv.nx), dtype=torch.float64).pin_memory().numpy() for _ in range(3)]
+        import ctypes as C
+        lib = _lib.lib()
+        L2 = C.c_double()
+        e2e_t = []
+        for it in range(max(2, args.steps)):
+            barrier()
+            t0 = time.perf_counter()
+            _lib.check(lib.psv_plan_set_model(p.h, *[_lib.dptr(a) for a in h_model]))
+            _lib.check(lib.psv_plan_set_observed(p.h, _lib.dptr(h_obs[0]), _lib.dptr(h_obs[1])))
+            _lib.check(lib.psv_gradient(p.h, C.byref(L2), *[_lib.dptr(a) for a in h_grad]))
+            if world > 1:
+                import torch.distributed as dist
+                g = torch.from_numpy(np.stack(h_grad)).cuda()
+                dist.all_reduce(g)
+            torch.cuda.synchronize()
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_s = float(np.mean(e2e_t[1:]))
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e2e_s], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = sum(a.nbytes for a in h_model) + sum(a.nbytes for a in h_obs)
+        d2h = sum(a.nbytes for a in h_grad) + 8
+
+        # ---- roofline of the dominant kernel (event-timed launches)
+        prof = p.profile_kernels(nsteps=min(300, nt))
+        fwi = None
+        if rank == 0 and not args.no_fwi:
+            t0 = time.perf_counter()
+            r = p.fwi_iteration(0.01)
+            fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
+
+    if rank != 0:
+        return None
+    shares = {k: v for k, v in prof.items() if not k.startswith("srcrec")}
+    top = max(shares, key=shares.get)
+    pts = CFG["nz"] * CFG["nx"] * nshot
+    alg = algorithmic_bytes(top, CFG["snap_dt"]) * pts
+    achieved = alg / (prof[top] * 1e-3) / 1e9
+    peak, src = peaks()
+    traffic = read_traffic(f"k_{top.split('_')[0]}_{top.split('_')[1]}")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model)",
+        "config": config_dict(world),
+        "shots_per_s": nshot * world / (ms / 1e3),
+        "split_ms": {k: round(v, 3) for k, v in split.items()},
+        "e2e": {"value": updates_per_step(nt, nshot) * world / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_s * 1e3},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": alg,
+                     "launch_ms": prof[top], "kernel_ms": {k: round(v, 5) for k, v in prof.items()}},
+        "gpu_launches": launches,
+        "clocks": clocks,
+    }
+    if fwi:
+        line["fwi_iteration_s"] = fwi["seconds"]
+        line["fwi_trials"] = fwi["trials"]
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
+    return line
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores: each
+    step is a bounded sample (one shot forward + adjoint, nt cropped)."""
+    for _ in range(args.warmup):
+        cpu_baseline(nt_sample=args.ref_nt)
+    vals = [cpu_baseline(nt_sample=args.ref_nt) for _ in range(args.steps)]
+    v = float(np.mean([x["value"] for x in vals]))
+    b = vals[-1]
+    upd = 2.0 * args.ref_nt * CFG["nz"] * CFG["nx"]
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": upd / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded layered model)", "config": config_dict(1),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": b["cores"], "kind": b["kind"],
+                             "sample": b["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-nt", type=int, default=1000)
+    ap.add_argument("--ref-nt", type=int, default=400)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fwi", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)), flush=True)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    line = run_ours(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,123 @@
+// psv_plan.cuh -- the device-resident survey plan (host C++ side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "fwi_psv.h"
+#include "psv_fwi.cuh"
+#include "psv_internal.h"
+#include "psv_kernels.cuh"
+
+namespace psv {
+
+template <typename T> cudaError_t launch_stress(const StepParams<T> &, int, dim3, int, cudaStream_t);
+template <typename T>
+cudaError_t launch_velocity(const StepParams<T> &, int, int, int, dim3, int, cudaStream_t);
+template <typename T>
+cudaError_t launch_srcrec(const StepParams<T> &, const SrcRecParams<T> &, int, int, int,
+                          cudaStream_t);
+template <typename T>
+cudaError_t launch_zero_planes(T *base, long long shot_stride, long long off, long long count,
+                               int nbatch, cudaStream_t st);
+cudaError_t launch_transpose(const double *in, double *out, int rows, int cols, int nbatch,
+                             cudaStream_t st);
+
+#define PSV_CU(call)                                                                        \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return ::psv::fail(PSV_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define PSV_TRY(call)                  \
+    do {                               \
+        int s_ = (call);               \
+        if (s_ != PSV_OK) return s_;   \
+    } while (0)
+
+// Validated host copy of a survey and the geometry derived from it.
+struct Survey {
+    psv_grid g{};
+    psv_shots s{};
+    std::vector<double> prof[12];  // a_z b_z K_z ah_z bh_z Kh_z a_x b_x K_x ah_x bh_x Kh_x
+    std::vector<int> z_src, x_src, fire, z_rec, x_rec;
+    std::vector<double> stf_z, stf_x;
+    int ns = 1, fpad = 1, nz1 = 0, nz2 = 0, nx1 = 0, nx2 = 0;
+    int pz0 = 0, pz1 = 0, px0 = 0, px1 = 0;  // identity (non-strip) ranges
+    int snt = 1, snz = 1, snx = 1;
+    int st = 0, sb = 0, sl = 0, sr = 0;
+};
+
+int make_survey(const psv_grid *g, const psv_shots *s, Survey &out);
+
+// Owning device allocation.
+struct DevMem {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevMem() = default;
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    ~DevMem() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    int alloc(size_t n, size_t &total)
+    {
+        release();
+        if (n == 0) return PSV_OK;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();
+            return fail(e == cudaErrorMemoryAllocation ? PSV_ERR_OOM : PSV_ERR_CUDA,
+                        std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+        }
+        bytes = n;
+        total += n;
+        return PSV_OK;
+    }
+    template <typename U> U *as() const { return static_cast<U *>(p); }
+};
+
+// Interface of a plan, independent of the wavefield precision.
+struct PlanIface {
+    virtual ~PlanIface() = default;
+    virtual long long device_bytes() const = 0;
+    virtual int set_model(const double *lam, const double *mu, const double *rho) = 0;
+    virtual int get_model(double *lam, double *mu, double *rho) = 0;
+    virtual int set_observed(const double *uz, const double *ux) = 0;
+    virtual int forward(double *uz, double *ux) = 0;
+    virtual int gradient(double *L2) = 0;
+    virtual int get_gradient(double *gl, double *gm, double *gr) = 0;
+    virtual int set_gradient(const double *gl, const double *gm, const double *gr) = 0;
+    virtual int reset_gradient() = 0;
+    virtual int get_shot(int ishot, double *gl, double *gm, double *gr, double *We, double *WeA,
+                         double *uz, double *ux, double *L2) = 0;
+    virtual int fwi_iteration(double *step, double *L2, int *ntrials, double *tlog, int maxt) = 0;
+    virtual int timing(double *ms3) const = 0;
+    virtual void *stream() const = 0;
+    virtual long long launches() const = 0;
+    virtual int profile(int nsteps, double *ms6) = 0;
+    // kernel_PSV drop-in support
+    virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
+                            const double *rho_zp, const double *rho_xp, int ishot, int grad,
+                            int accu, double *const *accu_in_out, double *const *fields_out,
+                            double *const *mem_out, double *rtf_uz, double *rtf_ux,
+                            double *const *grad_out) = 0;
+};
+
+std::unique_ptr<PlanIface> make_plan_f32(const Survey &sv, const psv_options &opt, int &status);
+std::unique_ptr<PlanIface> make_plan_f64(const Survey &sv, const psv_options &opt, int &status);
+
+}  // namespace psv
+
+struct psv_plan {
+    std::unique_ptr<psv::PlanIface> impl;
+};

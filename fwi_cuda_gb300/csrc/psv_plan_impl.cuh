@@ -1,0 +1,956 @@
+// psv_plan_impl.cuh -- Plan<T>: device layout, time loop and FWI drivers.
+// Instantiated for float (psv_plan_f32.cu) and double (psv_plan_f64.cu).
+#pragma once
+
+#include <cmath>
+#include <cstring>
+
+#include "psv_plan.cuh"
+
+namespace psv {
+
+inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// Which time loop a pass runs.
+enum PassKind {
+    PASS_FWD_STORE = 0,  // gradient forward: We + snapshots (kernel_PSV accu = true)
+    PASS_FWD_PLAIN = 1,  // modelling / step-length trials: traces only
+    PASS_ADJ_RES = 2,    // adjoint fired by the residuals at the receivers
+    PASS_FWD_U = 3,      // drop-in forward: u, We, optional snapshots (no graph)
+    PASS_ADJ_GIVEN = 4,  // drop-in adjoint with the caller's sources (no graph)
+    NPASS = 5
+};
+
+template <typename T>
+class Plan final : public PlanIface {
+public:
+    Survey sv;
+    psv_options opt;
+    int B = 1, nbatch = 1;
+    int pitch = 0, mx_pitch = 0, snx_pitch = 0, nzs = 0, nxs = 0;
+    long long plane = 0, shot_stride = 0, mz_shot = 0, mx_shot = 0, hist_shot = 0, gshot_shot = 0;
+    long long ntr = 0;  // nt * nrec
+    size_t total = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[4] = {};
+    int *h_ctl = nullptr;
+    DevMem fld, memz, memx, hist, gshot, coef, prof, fsb;
+    DevMem model, stf, traces, red, taperb, ctl, scales;
+    DevMem f_off, f_pos, f_col, f_snap, a_off, a_pos, a_col, a_snap, rec_pos;
+    StepParams<T> sp{};
+    SrcRecParams<T> qf{}, qa{}, qk{};
+    cudaGraphExec_t gx[NPASS] = {};
+    double C[3] = {0, 0, 0};
+    double inj = 1.0;     // dt/(dz dx) * max(1/rho): injection gain of a displacement source
+    double gscale = 1.0;  // power of two on the imaging factors g1, g2
+    std::vector<double> L2_shot;
+    int last_s0 = -1, last_n = 0, last_batch_s0 = 0;
+    double t_ms[3] = {0, 0, 0};
+    bool have_model = false, have_obs = false, store_flag = false;
+    long long nlaunch = 0;          // kernels launched (graph nodes counted per replay)
+    long long gx_nodes[NPASS] = {}; // kernels in each captured pass
+    dim3 blk{32, 8, 1};
+
+    ~Plan() override
+    {
+        for (auto &g : gx)
+            if (g) cudaGraphExecDestroy(g);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    long long device_bytes() const override { return (long long)total; }
+
+    double *dm(int k) const { return model.as<double>() + (size_t)k * sv.g.nz * sv.g.nx; }
+    double *lam() const { return dm(0); }
+    double *mu() const { return dm(1); }
+    double *rho() const { return dm(2); }
+    double *lamc() const { return dm(3); }
+    double *muc() const { return dm(4); }
+    double *rhoc() const { return dm(5); }
+    double *grad(int k) const { return dm(6 + k); }
+    double *avg(int k) const { return dm(9 + k); }
+    double *tr(int k) const { return traces.as<double>() + (size_t)k * sv.s.nshot * ntr; }
+    // traces: 0 rtf_z 1 rtf_x 2 obs_z 3 obs_x 4 res_z 5 res_x (all [shot][nt][nrec])
+    double *partial() const { return red.as<double>(); }
+    double *L2dev() const { return red.as<double>() + (size_t)256 * std::max(3, sv.s.nshot); }
+    double *cavg() const { return L2dev() + sv.s.nshot; }
+    double *wmax() const { return cavg() + 3; }
+    unsigned long long *maxbits() const { return (unsigned long long *)(wmax() + B); }
+    // scales: fscale[nshot] funscale[nshot] ascale[nshot] rmax_bits[nshot]
+    double *fscale() const { return scales.as<double>(); }
+    double *funscale() const { return fscale() + sv.s.nshot; }
+    double *ascale() const { return fscale() + 2 * sv.s.nshot; }
+    unsigned long long *rmax() const { return (unsigned long long *)(fscale() + 3 * sv.s.nshot); }
+
+    // ---------------------------------------------------------------- setup
+    int init(const Survey &s_, const psv_options &o)
+    {
+        sv = s_;
+        opt = o;
+        const psv_grid &g = sv.g;
+        const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
+        const int al = 128 / (int)sizeof(T);
+        if (opt.block_x > 0 && opt.block_y > 0 && opt.block_x * opt.block_y <= 256 &&
+            opt.block_x % 32 == 0)
+            blk = dim3(opt.block_x, opt.block_y, 1);
+        pitch = round_up(nx, al);
+        plane = (long long)nz * pitch;
+        shot_stride = NFIELD * plane;
+        nzs = g.pml_z ? sv.pz0 + (nz - sv.pz1) : 0;
+        nxs = g.pml_x ? sv.px0 + (nx - sv.px1) : 0;
+        mx_pitch = nxs ? round_up(nxs, al) : 0;
+        mz_shot = (long long)NMZ * nzs * pitch;
+        mx_shot = (long long)NMX * nz * mx_pitch;
+        snx_pitch = round_up(sv.snx, al);
+        const long long snap_plane = (long long)sv.snz * snx_pitch;
+        hist_shot = (long long)sv.snt * NHIST * snap_plane;
+        gshot_shot = 3 * snap_plane;
+        ntr = (long long)g.nt * nrec;
+
+        const double budget = (opt.hbm_budget_gb > 0 ? opt.hbm_budget_gb : 180.0) * 1e9;
+        const double per_shot = (double)(shot_stride + mz_shot + mx_shot + gshot_shot) * sizeof(T);
+        const double per_hist = (double)hist_shot * sizeof(T);
+        const double shared = 7.0 * plane * sizeof(T) + 12.0 * nz * nx * 8 + 6.0 * nshot * ntr * 8;
+        B = opt.max_batch > 0 ? std::min(opt.max_batch, nshot) : nshot;
+        while (B > 1 && shared + B * (per_shot + per_hist) > budget) B--;
+        if (shared + B * (per_shot + per_hist) > budget && opt.storage == PSV_STORE_FULL)
+            return fail(PSV_ERR_OOM, "full snapshot history of one shot exceeds the HBM budget");
+        nbatch = (nshot + B - 1) / B;
+
+        PSV_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        for (auto &e : ev) PSV_CU(cudaEventCreate(&e));
+        PSV_CU(cudaMallocHost(&h_ctl, sizeof(int) * 2 * nbatch));
+        for (int b = 0; b < nbatch; b++) {
+            h_ctl[2 * b] = b * B;
+            h_ctl[2 * b + 1] = std::min(B, nshot - b * B);
+        }
+
+        PSV_TRY(fld.alloc((size_t)B * shot_stride * sizeof(T), total));
+        PSV_TRY(memz.alloc((size_t)B * mz_shot * sizeof(T), total));
+        PSV_TRY(memx.alloc((size_t)B * mx_shot * sizeof(T), total));
+        PSV_TRY(gshot.alloc((size_t)B * gshot_shot * sizeof(T), total));
+        PSV_TRY(coef.alloc((size_t)7 * plane * sizeof(T), total));
+        const int nmax = std::max(nz, nx);
+        PSV_TRY(prof.alloc((size_t)12 * nmax * sizeof(T), total));
+        PSV_TRY(fsb.alloc((size_t)(2 * nx + 2 * nz) * sizeof(T), total));
+        PSV_TRY(model.alloc((size_t)12 * nz * nx * 8, total));
+        PSV_TRY(traces.alloc((size_t)6 * nshot * ntr * 8 + 8, total));
+        PSV_TRY(red.alloc(((size_t)256 * std::max(3, nshot) + nshot + 3 + B + 2) * 8, total));
+        PSV_TRY(taperb.alloc((size_t)(nx + nz) * 8, total));
+        PSV_TRY(ctl.alloc(2 * sizeof(int), total));
+        PSV_TRY(scales.alloc((size_t)4 * nshot * 8, total));
+        {
+            std::vector<double> one((size_t)3 * nshot, 1.0);
+            PSV_CU(cudaMemcpyAsync(scales.p, one.data(), one.size() * 8, cudaMemcpyHostToDevice, st));
+        }
+        PSV_CU(cudaMemsetAsync(model.p, 0, model.bytes, st));
+        PSV_CU(cudaMemsetAsync(fld.p, 0, fld.bytes, st));
+        PSV_CU(cudaMemsetAsync(coef.p, 0, coef.bytes, st));
+        PSV_CU(cudaMemsetAsync(fsb.p, 0, fsb.bytes, st));
+        PSV_CU(cudaMemsetAsync(traces.p, 0, traces.bytes, st));
+        PSV_CU(cudaMemcpyAsync(ctl.p, h_ctl, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+
+        PSV_TRY(upload_profiles());
+        PSV_TRY(upload_sources());
+        PSV_TRY(upload_taper());
+        fill_params();
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int upload_profiles()
+    {
+        const int nz = sv.g.nz, nx = sv.g.nx, nmax = std::max(nz, nx);
+        std::vector<T> h((size_t)12 * nmax, T(0));
+        for (int a = 0; a < 12; a++) {
+            const bool zaxis = a < 6;
+            const int n = zaxis ? nz : nx;
+            const bool on = zaxis ? sv.g.pml_z : sv.g.pml_x;
+            const int kind = a % 6;  // a b K a_half b_half K_half
+            for (int i = 0; i < n; i++) {
+                double v;
+                if (on) v = sv.prof[a][i];
+                else v = (kind == 1 || kind == 2 || kind == 4 || kind == 5) ? 1.0 : 0.0;
+                if (kind == 2 || kind == 5) v = 1.0 / v;  // store 1/K
+                h[(size_t)a * nmax + i] = (T)v;
+            }
+        }
+        PSV_CU(cudaMemcpyAsync(prof.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    // Forward sources grouped by the shot that fires them (vsrc2's
+    // src_shot_to_fire test), the adjoint's receivers per shot, receiver cells.
+    int upload_sources()
+    {
+        const int nshot = sv.s.nshot, nsrc = sv.s.nsrc, nrec = sv.s.nrec, nt = sv.g.nt;
+        std::vector<int> off(nshot + 1, 0), pos, col, snap;
+        for (int s = 0; s < nshot; s++) {
+            for (int is = 0; is < nsrc; is++)
+                if (sv.fire[is] == s) {
+                    pos.push_back(sv.z_src[is] * pitch + sv.x_src[is]);
+                    col.push_back(is);
+                    snap.push_back(snap_cell(sv.z_src[is], sv.x_src[is]));
+                }
+            off[s + 1] = (int)pos.size();
+        }
+        PSV_TRY(put(f_off, off));
+        PSV_TRY(put(f_pos, pos));
+        PSV_TRY(put(f_col, col));
+        PSV_TRY(put(f_snap, snap));
+        std::vector<int> aoff(nshot + 1), apos, acol, asnap, rpos(nrec);
+        for (int r = 0; r < nrec; r++) rpos[r] = sv.z_rec[r] * pitch + sv.x_rec[r];
+        for (int s = 0; s < nshot; s++) {
+            aoff[s] = s * nrec;
+            for (int r = 0; r < nrec; r++) {
+                apos.push_back(rpos[r]);
+                acol.push_back(r);
+                asnap.push_back(-1);
+            }
+        }
+        aoff[nshot] = nshot * nrec;
+        PSV_TRY(put(a_off, aoff));
+        PSV_TRY(put(a_pos, apos));
+        PSV_TRY(put(a_col, acol));
+        PSV_TRY(put(a_snap, asnap));
+        PSV_TRY(put(rec_pos, rpos));
+        // stf [nsrc][nt] -> [nt][nsrc]
+        std::vector<double> h((size_t)2 * nt * std::max(nsrc, 1), 0.0);
+        for (int is = 0; is < nsrc; is++)
+            for (int it = 0; it < nt; it++) {
+                h[(size_t)it * nsrc + is] = sv.stf_z[(size_t)is * nt + it];
+                h[(size_t)nt * nsrc + (size_t)it * nsrc + is] = sv.stf_x[(size_t)is * nt + it];
+            }
+        PSV_TRY(stf.alloc(h.size() * 8, total));
+        PSV_CU(cudaMemcpyAsync(stf.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int snap_cell(int iz, int ix) const
+    {
+        const psv_grid &g = sv.g;
+        const int dz = iz - g.snap_z1, dx = ix - g.snap_x1;
+        if (dz < 0 || iz > g.snap_z2 || dx < 0 || ix > g.snap_x2) return -1;
+        if (dz % g.snap_dz || dx % g.snap_dx) return -1;
+        return (dz / g.snap_dz) * snx_pitch + dx / g.snap_dx;
+    }
+
+    template <typename V> int put(DevMem &m, const std::vector<V> &v)
+    {
+        PSV_TRY(m.alloc(std::max<size_t>(v.size(), 1) * sizeof(V), total));
+        if (!v.empty())
+            PSV_CU(cudaMemcpyAsync(m.p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    // taper2's horizontal and vertical factors (src/cpu/n_kernel_lib_PSV.cpp:949-1009).
+    int upload_taper()
+    {
+        const psv_grid &g = sv.g;
+        const int nz = g.nz, nx = g.nx;
+        const int t1 = g.taper[0], t2 = g.taper[1], b1 = g.taper[2], b2 = g.taper[3];
+        const int l1 = g.taper[4], l2 = g.taper[5], r1 = g.taper[6], r2 = g.taper[7];
+        const int tl = l2 - l1, trr = r1 - r2, tt = t2 - t1, tb = b1 - b2;
+        const double PI_REF = 3.14159265;
+        std::vector<double> h((size_t)nx + nz, 1.0);
+        for (int ix = 0; ix < nx; ix++) {
+            double f = 1.0;
+            if (ix >= g.snap_x1 && ix < l1) f = 0.0;
+            else if (ix >= l1 && ix < l2) f = 0.5 * (1.0 - cos(PI_REF * (ix - l1) / tl));
+            else if (ix > r2 && ix < r1) f = 0.5 * (1.0 - cos(PI_REF * (r1 - ix) / trr));
+            else if (ix >= r1 && ix <= g.snap_x2) f = 0.0;
+            h[ix] = f;
+        }
+        for (int iz = 0; iz < nz; iz++) {
+            double f = 1.0;
+            if (iz >= g.snap_z1 && iz < t1) f = 0.0;
+            else if (iz >= t1 && iz < t2) f = 0.5 * (1.0 - cos(PI_REF * (iz - t1) / tt));
+            else if (iz > b2 && iz < b1) f = 0.5 * (1.0 - cos(PI_REF * (b1 - iz) / tb));
+            else if (iz >= b1 && iz <= g.snap_z2) f = 0.0;
+            h[(size_t)nx + iz] = f;
+        }
+        PSV_CU(cudaMemcpyAsync(taperb.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    void fill_params()
+    {
+        const psv_grid &g = sv.g;
+        const int nz = g.nz, nx = g.nx, nmax = std::max(nz, nx);
+        StepParams<T> &p = sp;
+        p = StepParams<T>{};
+        p.nz = nz; p.nx = nx; p.pitch = pitch;
+        p.nz1 = sv.nz1; p.nz2 = sv.nz2; p.nx1 = sv.nx1; p.nx2 = sv.nx2;
+        p.plane = plane; p.shot_stride = shot_stride;
+        p.fld = fld.as<T>();
+        const double dzi = 1.0 / g.dz, dxi = 1.0 / g.dx;
+        for (int k = 0; k < 4; k++) {
+            p.cz[k] = k < sv.ns ? (T)(dzi * g.hc[k + 1]) : T(0);
+            p.cx[k] = k < sv.ns ? (T)(dxi * g.hc[k + 1]) : T(0);
+        }
+        p.dt = (T)g.dt;
+        p.inv_dt = (T)(1.0 / g.dt);
+        p.kimg = (T)(g.snap_dt * g.dt);
+        p.pml_z = g.pml_z; p.pml_x = g.pml_x;
+        p.pz0 = g.pml_z ? sv.pz0 : 0; p.pz1 = g.pml_z ? sv.pz1 : nz;
+        p.px0 = g.pml_x ? sv.px0 : 0; p.px1 = g.pml_x ? sv.px1 : nx;
+        p.mx_pitch = mx_pitch;
+        p.mz_plane = (long long)nzs * pitch; p.mz_shot_stride = mz_shot;
+        p.mx_plane = (long long)nz * mx_pitch; p.mx_shot_stride = mx_shot;
+        p.memz = memz.as<T>(); p.memx = memx.as<T>();
+        const T *pr = prof.as<T>();
+        p.a_z = pr + 0 * nmax; p.b_z = pr + 1 * nmax; p.ki_z = pr + 2 * nmax;
+        p.ah_z = pr + 3 * nmax; p.bh_z = pr + 4 * nmax; p.khi_z = pr + 5 * nmax;
+        p.a_x = pr + 6 * nmax; p.b_x = pr + 7 * nmax; p.ki_x = pr + 8 * nmax;
+        p.ah_x = pr + 9 * nmax; p.bh_x = pr + 10 * nmax; p.khi_x = pr + 11 * nmax;
+        T *c = coef.as<T>();
+        p.c_lam = c; p.c_l2m = c + plane; p.c_muzx = c + 2 * plane; p.c_rz = c + 3 * plane;
+        p.c_rx = c + 4 * plane; p.g1 = c + 5 * plane; p.g2 = c + 6 * plane;
+        p.st = sv.st; p.sb = sv.sb; p.sl = sv.sl; p.sr = sv.sr;
+        T *fs = fsb.as<T>();
+        p.fs_top = fs; p.fs_bot = fs + nx; p.fs_left = fs + 2 * nx; p.fs_right = fs + 2 * nx + nz;
+        p.snap_z1 = g.snap_z1; p.snap_z2 = g.snap_z2; p.snap_x1 = g.snap_x1; p.snap_x2 = g.snap_x2;
+        p.snap_dz = g.snap_dz; p.snap_dx = g.snap_dx;
+        p.snz = sv.snz; p.snx = sv.snx; p.snx_pitch = snx_pitch;
+        p.snap_plane = (long long)sv.snz * snx_pitch;
+        p.hist_slot_stride = NHIST * p.snap_plane;
+        p.hist_shot_stride = hist_shot;
+        p.hist = hist.as<T>();
+        p.gshot = gshot.as<T>();
+        p.gshot_shot_stride = gshot_shot;
+        p.ctl = ctl.as<int>();
+
+        SrcRecParams<T> q{};
+        q.src_off = f_off.as<int>(); q.src_pos = f_pos.as<int>(); q.src_col = f_col.as<int>();
+        q.src_snap = f_snap.as<int>();
+        q.stf_z = stf.as<double>();
+        q.stf_x = stf.as<double>() + (size_t)g.nt * sv.s.nsrc;
+        q.stf_shot_stride = 0; q.stf_ncol = sv.s.nsrc; q.stf_type = sv.s.stf_type;
+        q.inv_dzdx = 1.0 / (g.dz * g.dx);
+        q.nrec = sv.s.nrec; q.rec_pos = rec_pos.as<int>();
+        q.rtf_z = sv.s.rtf_type == 0 ? tr(0) : nullptr;
+        q.rtf_x = sv.s.rtf_type == 0 ? tr(1) : nullptr;
+        q.rtf_shot_stride = ntr;
+        q.dt_d = g.dt; q.dzdx = g.dz * g.dx; q.nt = g.nt;
+        q.amp_scale = fscale(); q.rec_unscale = funscale();
+        qf = q;
+        qk = q;  // drop-in adjoint: the caller's sources, no recording
+        qk.rtf_z = qk.rtf_x = nullptr;
+        qa = q;  // FWI adjoint: residuals fired at the receivers (adjoint call, n_simulate_PSV.cpp:344-356)
+        qa.src_off = a_off.as<int>(); qa.src_pos = a_pos.as<int>(); qa.src_col = a_col.as<int>();
+        qa.src_snap = a_snap.as<int>();
+        qa.stf_z = tr(4); qa.stf_x = tr(5);
+        qa.stf_shot_stride = ntr; qa.stf_ncol = sv.s.nrec; qa.stf_type = sv.s.rtf_type;
+        qa.rtf_z = qa.rtf_x = nullptr;
+        qa.amp_scale = ascale();
+    }
+
+    int ensure_hist()
+    {
+        if (hist.p || hist_shot == 0) return PSV_OK;
+        PSV_TRY(hist.alloc((size_t)B * hist_shot * sizeof(T), total));
+        sp.hist = hist.as<T>();
+        drop_graphs();
+        return PSV_OK;
+    }
+
+    void drop_graphs()
+    {
+        for (auto &g : gx)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+
+    // ----------------------------------------------------------- time loop
+    int enqueue(int kind)
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        const bool adj = kind == PASS_ADJ_RES || kind == PASS_ADJ_GIVEN;
+        const bool store = kind == PASS_FWD_STORE || (kind == PASS_FWD_U && store_flag);
+        const int mode = kind == PASS_FWD_STORE ? MODE_FWD
+                         : kind == PASS_FWD_PLAIN ? MODE_FWD_NOWE
+                         : kind == PASS_FWD_U ? MODE_FWD_U : MODE_ADJ;
+        const SrcRecParams<T> &q = kind == PASS_ADJ_RES ? qa : kind == PASS_ADJ_GIVEN ? qk : qf;
+        T *f = fld.as<T>();
+        const long long n0 = nlaunch;
+        // reset_sv2 / reset_PML_memory2 / reset_grad_shot2 (n_kernel_PSV.cpp:74-88)
+        if (mode == MODE_ADJ) {
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 7 * plane, B, st));
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WEA * plane, plane, B, st));
+            PSV_CU(launch_zero_planes<T>(gshot.as<T>(), gshot_shot, 0, gshot_shot, B, st));
+        } else if (mode == MODE_FWD_U) {
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 8 * plane, B, st));
+        } else {
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
+            if (mode == MODE_FWD)
+                PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WE * plane, plane, B, st));
+        }
+        PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+        PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+        for (int jt = 0; jt < nt; jt++) {
+            const int it = adj ? nt - 1 - jt : jt;
+            const bool snap = !(it % sdt);
+            PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
+            PSV_CU(launch_velocity<T>(sp, sv.ns, mode, (snap && (store || adj)) ? it / sdt : -1, blk,
+                                      B, st));
+            PSV_CU(launch_srcrec<T>(sp, q, it, (snap && store) ? it / sdt : -1, B, st));
+        }
+        nlaunch = n0 + 3LL * nt + (mode == MODE_ADJ ? 5 : mode == MODE_FWD ? 4 : 3);
+        return PSV_OK;
+    }
+
+    int run_pass(int kind)
+    {
+        const bool graphable = kind == PASS_FWD_STORE || kind == PASS_FWD_PLAIN || kind == PASS_ADJ_RES;
+        if (!opt.use_graphs || !graphable) return enqueue(kind);
+        if (!gx[kind]) {
+            cudaGraph_t graph = nullptr;
+            PSV_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            const long long n0 = nlaunch;
+            const int s = enqueue(kind);
+            gx_nodes[kind] = nlaunch - n0;
+            nlaunch = n0;
+            cudaError_t e = cudaStreamEndCapture(st, &graph);
+            if (s != PSV_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return s;
+            }
+            if (e != cudaSuccess) return fail(PSV_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&gx[kind], graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                gx[kind] = nullptr;
+                return fail(PSV_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+            }
+        }
+        PSV_CU(cudaGraphLaunch(gx[kind], st));
+        nlaunch += gx_nodes[kind];
+        return PSV_OK;
+    }
+
+    int set_batch(int b)
+    {
+        PSV_CU(cudaMemcpyAsync(ctl.p, h_ctl + 2 * b, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+        return PSV_OK;
+    }
+
+    // --------------------------------------------------------------- model
+    int coefficients(bool sums, bool given_avg)
+    {
+        CoeffParams<T> c{};
+        c.nz = sv.g.nz; c.nx = sv.g.nx; c.pitch = pitch;
+        c.dt = sv.g.dt; c.kimg = (double)sv.g.snap_dt * sv.g.dt; c.gscale = gscale;
+        c.lam = lam(); c.mu = mu(); c.rho = rho();
+        if (given_avg) { c.mu_zx = avg(0); c.rho_zp = avg(1); c.rho_xp = avg(2); }
+        c.c_lam = (T *)sp.c_lam; c.c_l2m = (T *)sp.c_l2m; c.c_muzx = (T *)sp.c_muzx;
+        c.c_rz = (T *)sp.c_rz; c.c_rx = (T *)sp.c_rx; c.g1 = (T *)sp.g1; c.g2 = (T *)sp.g2;
+        c.st = sv.st; c.sb = sv.sb; c.sl = sv.sl; c.sr = sv.sr;
+        c.fs_top = (T *)sp.fs_top; c.fs_bot = (T *)sp.fs_bot;
+        c.fs_left = (T *)sp.fs_left; c.fs_right = (T *)sp.fs_right;
+        PSV_CU(launch_coeffs<T>(c, st));
+        if (sums) {
+            PSV_CU(launch_model_sums(lam(), mu(), rho(), sv.g.nz, sv.g.nx, partial(), cavg(), st));
+            double h[3];
+            PSV_CU(cudaMemcpyAsync(h, cavg(), sizeof(h), cudaMemcpyDeviceToHost, st));
+            PSV_CU(cudaStreamSynchronize(st));
+            const double cnt = (double)((sv.g.nz - 1) * (sv.g.nx - 1));
+            for (int k = 0; k < 3; k++) C[k] = h[k] / cnt;
+        }
+        return PSV_OK;
+    }
+
+    static double pow2_near(double x) { return (x > 0 && std::isfinite(x)) ? std::exp2(-std::rint(std::log2(x))) : 1.0; }
+
+    // Range scales from a host model: forward source gain (exact powers of two).
+    void model_scales(const double *l, const double *m, double inv_rho_max)
+    {
+        const psv_grid &g = sv.g;
+        const size_t n = (size_t)g.nz * g.nx;
+        inj = g.dt / (g.dz * g.dx) * inv_rho_max;
+        double amax = 0.0;
+        for (double v : sv.stf_z) amax = std::max(amax, std::fabs(v));
+        for (double v : sv.stf_x) amax = std::max(amax, std::fabs(v));
+        const double sf = pow2_near(sv.s.stf_type == 0 ? amax * inj : amax);
+        // imaging factor: g1 * (dt (lam + 2 mu) / dz)^2 ~ 1 with unit-scaled fields
+        double g1max = 0.0, cmax = 0.0;
+        const double kimg = (double)g.snap_dt * g.dt;
+        for (size_t k = 0; k < n; k++) {
+            const double lm = l[k] + m[k];
+            if (lm > 0) g1max = std::max(g1max, kimg * 0.25 / (lm * lm));
+            cmax = std::max(cmax, g.dt * (l[k] + 2.0 * m[k]) / std::min(g.dz, g.dx));
+        }
+        gscale = pow2_near(g1max * cmax * cmax);
+        std::vector<double> h((size_t)2 * sv.s.nshot);
+        for (int s_ = 0; s_ < sv.s.nshot; s_++) { h[s_] = sf; h[sv.s.nshot + s_] = 1.0 / sf; }
+        cudaMemcpyAsync(fscale(), h.data(), h.size() * 8, cudaMemcpyHostToDevice, st);
+    }
+
+    int set_model(const double *l, const double *m, const double *r) override
+    {
+        const size_t n = (size_t)sv.g.nz * sv.g.nx;
+        double rmin = 0.0;
+        for (size_t k = 0; k < n; k++)
+            if (r[k] > 1e-4 && (rmin == 0.0 || r[k] < rmin)) rmin = r[k];
+        model_scales(l, m, rmin > 0 ? 1.0 / rmin : 1.0);
+        PSV_CU(cudaMemcpyAsync(lam(), l, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(mu(), m, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(rho(), r, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_TRY(coefficients(true, false));
+        have_model = true;
+        return PSV_OK;
+    }
+
+    int get_model(double *l, double *m, double *r) override
+    {
+        const size_t n = (size_t)sv.g.nz * sv.g.nx;
+        if (l) PSV_CU(cudaMemcpyAsync(l, lam(), n * 8, cudaMemcpyDeviceToHost, st));
+        if (m) PSV_CU(cudaMemcpyAsync(m, mu(), n * 8, cudaMemcpyDeviceToHost, st));
+        if (r) PSV_CU(cudaMemcpyAsync(r, rho(), n * 8, cudaMemcpyDeviceToHost, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    // Host traces [nshot][nrec][nt] <-> device [nshot][nt][nrec] through the
+    // residual buffer used as staging.
+    int upload_traces(double *dst, const double *src)
+    {
+        const int nshot = sv.s.nshot;
+        PSV_CU(cudaMemcpyAsync(tr(4), src, (size_t)nshot * ntr * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(launch_transpose(tr(4), dst, sv.s.nrec, sv.g.nt, nshot, st));
+        return PSV_OK;
+    }
+
+    int download_traces(double *dst, const double *src, int s0, int n)
+    {
+        PSV_CU(launch_transpose(src + (size_t)s0 * ntr, tr(5), sv.g.nt, sv.s.nrec, n, st));
+        PSV_CU(cudaMemcpyAsync(dst, tr(5), (size_t)n * ntr * 8, cudaMemcpyDeviceToHost, st));
+        return PSV_OK;
+    }
+
+    int set_observed(const double *uz, const double *ux) override
+    {
+        if (sv.s.nrec == 0) return fail(PSV_ERR_ARG, "survey has no receivers");
+        PSV_TRY(upload_traces(tr(2), uz));
+        PSV_TRY(upload_traces(tr(3), ux));
+        PSV_CU(cudaStreamSynchronize(st));
+        have_obs = true;
+        return PSV_OK;
+    }
+
+    // ------------------------------------------------------------ drivers
+    int forward(double *uz, double *ux) override
+    {
+        if (!have_model) return fail(PSV_ERR_ARG, "forward: no model set");
+        PSV_CU(cudaEventRecord(ev[0], st));
+        for (int b = 0; b < nbatch; b++) {
+            PSV_TRY(set_batch(b));
+            PSV_TRY(run_pass(PASS_FWD_PLAIN));
+        }
+        PSV_CU(cudaEventRecord(ev[1], st));
+        if (uz && sv.s.nrec) PSV_TRY(download_traces(uz, tr(0), 0, sv.s.nshot));
+        if (ux && sv.s.nrec) PSV_TRY(download_traces(ux, tr(1), 0, sv.s.nshot));
+        PSV_CU(cudaStreamSynchronize(st));
+        float ms = 0;
+        PSV_CU(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        t_ms[0] = ms; t_ms[1] = 0; t_ms[2] = 0;
+        return PSV_OK;
+    }
+
+    // Forward + residual + adjoint + preconditioning of every shot
+    // (src/cpu/n_simulate_PSV.cpp:270-419), batch by batch in shot order.
+    int gradient(double *L2) override
+    {
+        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "gradient: model and observed traces required");
+        PSV_TRY(ensure_hist());
+        PSV_TRY(coefficients(true, false));
+        const int nshot = sv.s.nshot;
+        double tf = 0, ta = 0, to = 0;
+        for (int b = 0; b < nbatch; b++) {
+            const int s0 = b * B, n = std::min(B, nshot - s0);
+            PSV_TRY(set_batch(b));
+            last_batch_s0 = s0;
+            PSV_CU(cudaEventRecord(ev[0], st));
+            PSV_TRY(run_pass(PASS_FWD_STORE));
+            PSV_CU(cudaEventRecord(ev[1], st));
+            PSV_CU(launch_adjsrc(tr(0) + s0 * ntr, tr(1) + s0 * ntr, tr(2) + s0 * ntr,
+                                 tr(3) + s0 * ntr, tr(4) + s0 * ntr, tr(5) + s0 * ntr, ntr, n,
+                                 sv.g.dt, partial(), L2dev() + s0, st));
+            PSV_CU(launch_adjoint_scale(tr(4) + s0 * ntr, tr(5) + s0 * ntr, ntr, n, inj,
+                                        rmax() + s0, ascale() + s0, st));
+            PSV_CU(cudaEventRecord(ev[2], st));
+            PSV_TRY(run_pass(PASS_ADJ_RES));
+            PSV_CU(cudaEventRecord(ev[3], st));
+            PSV_TRY(precondition(n));
+            PSV_CU(cudaStreamSynchronize(st));
+            float a, c, d;
+            PSV_CU(cudaEventElapsedTime(&a, ev[0], ev[1]));
+            PSV_CU(cudaEventElapsedTime(&c, ev[1], ev[2]));
+            PSV_CU(cudaEventElapsedTime(&d, ev[2], ev[3]));
+            tf += a; to += c; ta += d;
+            last_s0 = s0;
+            last_n = n;
+        }
+        L2_shot.assign(nshot, 0.0);
+        PSV_CU(cudaMemcpy(L2_shot.data(), L2dev(), nshot * 8, cudaMemcpyDeviceToHost));
+        double s = 0.0;
+        for (int i = 0; i < nshot; i++) s += L2_shot[i];
+        if (L2) *L2 = s;
+        t_ms[0] = tf; t_ms[1] = ta; t_ms[2] = to;
+        return PSV_OK;
+    }
+
+    // energy_weights2 + interpol_grad2 + scale_grad_E2 (n_simulate_PSV.cpp:385-417).
+    int precondition(int n)
+    {
+        const psv_grid &g = sv.g;
+        PSV_CU(cudaMemsetAsync(wmax(), 0, B * 8, st));
+        PSV_CU(launch_energy_max<T>(fld.as<T>(), plane, shot_stride, pitch, g.snap_z1, g.snap_z2,
+                                    g.snap_x1, g.snap_x2, n, wmax(), st));
+        ScaleParams<T> s{};
+        s.nz = g.nz; s.nx = g.nx; s.pitch = pitch;
+        s.z1 = g.snap_z1; s.z2 = g.snap_z2; s.x1 = g.snap_x1; s.x2 = g.snap_x2;
+        s.sdz = g.snap_dz; s.sdx = g.snap_dx; s.snx_pitch = snx_pitch;
+        s.snap_plane = sp.snap_plane;
+        s.gshot = gshot.as<T>(); s.gshot_shot_stride = gshot_shot;
+        s.fld = fld.as<T>(); s.plane = plane; s.shot_stride = shot_stride;
+        s.wmax = wmax();
+        s.fscale = fscale(); s.ascale = ascale(); s.s0 = last_batch_s0;
+        const double sg = sv.g.imaging_sign > 0 ? -1.0 : 1.0;  // kernels accumulate the CPU sign
+        s.gun[0] = s.gun[1] = sg / gscale; s.gun[2] = sg;
+        for (int k = 0; k < 3; k++) { s.C[k] = C[k]; s.grad[k] = grad(k); }
+        s.nbatch = n;
+        PSV_CU(launch_scale<T>(s, st));
+        return PSV_OK;
+    }
+
+    int get_gradient(double *gl, double *gm, double *gr) override
+    {
+        const size_t n = (size_t)sv.g.nz * sv.g.nx;
+        double *o[3] = {gl, gm, gr};
+        for (int k = 0; k < 3; k++)
+            if (o[k]) PSV_CU(cudaMemcpyAsync(o[k], grad(k), n * 8, cudaMemcpyDeviceToHost, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int set_gradient(const double *gl, const double *gm, const double *gr) override
+    {
+        const size_t n = (size_t)sv.g.nz * sv.g.nx;
+        const double *in[3] = {gl, gm, gr};
+        for (int k = 0; k < 3; k++)
+            if (in[k]) PSV_CU(cudaMemcpyAsync(grad(k), in[k], n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int reset_gradient() override
+    {
+        PSV_CU(cudaMemsetAsync(grad(0), 0, (size_t)3 * sv.g.nz * sv.g.nx * 8, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int get_shot(int ishot, double *gl, double *gm, double *gr, double *We, double *WeA,
+                 double *uz, double *ux, double *L2) override
+    {
+        if (ishot < last_s0 || ishot >= last_s0 + last_n)
+            return fail(PSV_ERR_ARG, "get_shot_gradient: shot not in the last gradient batch");
+        const int b = ishot - last_s0;
+        const psv_grid &g = sv.g;
+        double sf = 1, sa = 1;
+        PSV_CU(cudaMemcpy(&sf, fscale() + ishot, 8, cudaMemcpyDeviceToHost));
+        PSV_CU(cudaMemcpy(&sa, ascale() + ishot, 8, cudaMemcpyDeviceToHost));
+        const double sg = sv.g.imaging_sign > 0 ? -1.0 : 1.0;
+        const double gun[3] = {sg / (gscale * sf * sa), sg / (gscale * sf * sa), sg / (sf * sa)};
+        std::vector<T> h((size_t)gshot_shot);
+        PSV_CU(cudaMemcpy(h.data(), gshot.as<T>() + b * gshot_shot, h.size() * sizeof(T),
+                          cudaMemcpyDeviceToHost));
+        double *o[3] = {gl, gm, gr};
+        for (int k = 0; k < 3; k++)
+            if (o[k])
+                for (int jz = 0; jz < sv.snz; jz++)
+                    for (int jx = 0; jx < sv.snx; jx++)
+                        o[k][(size_t)jz * sv.snx + jx] =
+                            (double)h[k * sp.snap_plane + (size_t)jz * snx_pitch + jx] * gun[k];
+        double *w[2] = {We, WeA};
+        const int wp[2] = {F_WE, F_WEA};
+        const double wun[2] = {1.0 / (sf * sf), 1.0 / (sa * sa)};
+        std::vector<T> pl((size_t)plane);
+        for (int k = 0; k < 2; k++) {
+            if (!w[k]) continue;
+            PSV_CU(cudaMemcpy(pl.data(), fld.as<T>() + b * shot_stride + wp[k] * plane,
+                              plane * sizeof(T), cudaMemcpyDeviceToHost));
+            for (int iz = 0; iz < g.nz; iz++)
+                for (int ix = 0; ix < g.nx; ix++)
+                    w[k][(size_t)iz * g.nx + ix] = (double)pl[(size_t)iz * pitch + ix] * wun[k];
+        }
+        if (uz) PSV_TRY(download_traces(uz, tr(0), ishot, 1));
+        if (ux) PSV_TRY(download_traces(ux, tr(1), ishot, 1));
+        PSV_CU(cudaStreamSynchronize(st));
+        if (L2) *L2 = L2_shot.empty() ? 0.0 : L2_shot[ishot];
+        return PSV_OK;
+    }
+
+    // ---------------------------------------------------------- FWI step
+    // Trial forward of every shot for a candidate step (step_length_PSV's
+    // inner loop, src/cpu/n_step_length_PSV.cpp:87-123).
+    int trial(double est, double *L2)
+    {
+        const int n = sv.g.nz * sv.g.nx;
+        unsigned long long *mb = maxbits();
+        PSV_CU(launch_update_mat(lam(), lamc(), grad(0), n, 4.8e+10, 0.0, est, mb, st));
+        PSV_CU(launch_update_mat(mu(), muc(), grad(1), n, 2.7e+10, 0.0, est, mb, st));
+        PSV_CU(launch_update_mat(rho(), rhoc(), grad(2), n, 3000.0, 1.5, 0.5 * est, mb, st));
+        PSV_TRY(coefficients(false, false));
+        for (int b = 0; b < nbatch; b++) {
+            const int s0 = b * B, nb = std::min(B, sv.s.nshot - s0);
+            PSV_TRY(set_batch(b));
+            PSV_TRY(run_pass(PASS_FWD_PLAIN));
+            PSV_CU(launch_adjsrc(tr(0) + s0 * ntr, tr(1) + s0 * ntr, tr(2) + s0 * ntr,
+                                 tr(3) + s0 * ntr, nullptr, nullptr, ntr, nb, sv.g.dt, partial(),
+                                 L2dev() + s0, st));
+        }
+        std::vector<double> h(sv.s.nshot);
+        PSV_CU(cudaMemcpyAsync(h.data(), L2dev(), h.size() * 8, cudaMemcpyDeviceToHost, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        double s = 0.0;
+        for (double v : h) s += v;
+        *L2 = s;
+        return PSV_OK;
+    }
+
+    int fwi_iteration(double *step, double *L2out, int *ntrials, double *tlog, int maxt) override
+    {
+        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "fwi_iteration: model and observed traces required");
+        const size_t n = (size_t)sv.g.nz * sv.g.nx;
+        // copy_mat (n_simulate_PSV.cpp:263)
+        PSV_CU(cudaMemcpyAsync(lamc(), lam(), n * 8, cudaMemcpyDeviceToDevice, st));
+        PSV_CU(cudaMemcpyAsync(muc(), mu(), n * 8, cudaMemcpyDeviceToDevice, st));
+        PSV_CU(cudaMemcpyAsync(rhoc(), rho(), n * 8, cudaMemcpyDeviceToDevice, st));
+        double L2 = 0;
+        PSV_TRY(gradient(&L2));
+        if (L2out) *L2out = L2;
+        const double t_grad = t_ms[0] + t_ms[1] + t_ms[2];
+        PSV_CU(cudaEventRecord(ev[0], st));
+        for (int k = 0; k < 3; k++)  // taper2 x3 (:443-450)
+            PSV_CU(launch_taper(grad(k), sv.g.nz, sv.g.nx, taperb.as<double>(),
+                                taperb.as<double>() + sv.g.nx, st));
+
+        // step_length_PSV (src/cpu/n_step_length_PSV.cpp:53-209), update_param 0.
+        double est = *step;
+        auto fn = [](double a, double *L, void *ctx) -> int {
+            return static_cast<Plan<T> *>(ctx)->trial(a, L);
+        };
+        const int rc = psv_step_length(&est, L2, fn, this, ntrials, tlog, maxt);
+        if (rc != PSV_OK) return rc;
+        *step = est;
+        // update_mat2 x3 (n_simulate_PSV.cpp:542-546)
+        const int ni = (int)n;
+        PSV_CU(launch_update_mat(lam(), lamc(), grad(0), ni, 4.8e+10, 0.0, est, maxbits(), st));
+        PSV_CU(launch_update_mat(mu(), muc(), grad(1), ni, 2.7e+10, 0.0, est, maxbits(), st));
+        PSV_CU(launch_update_mat(rho(), rhoc(), grad(2), ni, 3000.0, 1.25, 0.5 * est, maxbits(), st));
+        PSV_CU(cudaEventRecord(ev[1], st));
+        PSV_CU(cudaStreamSynchronize(st));
+        float ms = 0;
+        PSV_CU(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        t_ms[2] += ms;
+        (void)t_grad;
+        return PSV_OK;
+    }
+
+    int timing(double *ms3) const override
+    {
+        for (int k = 0; k < 3; k++) ms3[k] = t_ms[k];
+        return PSV_OK;
+    }
+
+    void *stream() const override { return (void *)st; }
+    long long launches() const override { return nlaunch; }
+
+    // Per-kernel event timing of nsteps forward then nsteps adjoint steps.
+    int profile(int nsteps, double *ms6) override
+    {
+        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "profile: model and observed traces required");
+        if (nsteps <= 0 || nsteps > sv.g.nt) return fail(PSV_ERR_ARG, "profile: nsteps must be in [1, nt]");
+        PSV_TRY(ensure_hist());
+        PSV_TRY(coefficients(true, false));
+        PSV_TRY(set_batch(0));
+        std::vector<cudaEvent_t> e((size_t)8 * nsteps, nullptr);
+        for (auto &x : e) PSV_CU(cudaEventCreate(&x));
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        T *f = fld.as<T>();
+        PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, (long long)NFIELD * plane, B, st));
+        PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+        PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+        int rc = PSV_OK;
+        for (int pass = 0; pass < 2 && rc == PSV_OK; pass++) {
+            const bool adj = pass == 1;
+            const SrcRecParams<T> &q = adj ? qa : qf;
+            for (int j = 0; j < nsteps; j++) {
+                const int it = adj ? nt - 1 - j : j;
+                const int slot = !(it % sdt) ? it / sdt : -1;
+                cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
+                cudaEventRecord(E[0], st);
+                cudaError_t c = launch_stress<T>(sp, sv.ns, blk, B, st);
+                cudaEventRecord(E[1], st);
+                if (c == cudaSuccess) c = launch_velocity<T>(sp, sv.ns, adj ? MODE_ADJ : MODE_FWD, slot, blk, B, st);
+                cudaEventRecord(E[2], st);
+                if (c == cudaSuccess) c = launch_srcrec<T>(sp, q, it, adj ? -1 : slot, B, st);
+                cudaEventRecord(E[3], st);
+                if (c != cudaSuccess) { rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c)); break; }
+                nlaunch += 3;
+            }
+        }
+        if (rc == PSV_OK) {
+            cudaError_t c = cudaStreamSynchronize(st);
+            if (c != cudaSuccess) rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c));
+        }
+        for (int k = 0; k < 6; k++) ms6[k] = 0.0;
+        if (rc == PSV_OK)
+            for (int pass = 0; pass < 2; pass++)
+                for (int j = 0; j < nsteps; j++) {
+                    cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
+                    for (int k = 0; k < 3; k++) {
+                        float ms = 0;
+                        cudaEventElapsedTime(&ms, E[k], E[k + 1]);
+                        ms6[pass * 3 + k] += ms / nsteps;
+                    }
+                }
+        for (auto &x : e) cudaEventDestroy(x);
+        return rc;
+    }
+
+    // ------------------------------------------------------- drop-in call
+    int kernel_call(const double *l, const double *m, const double *mzx, const double *rzp,
+                    const double *rxp, int ishot, int grad_, int accu, double *const *accu_io,
+                    double *const *fields_out, double *const *mem_out, double *rtf_uz,
+                    double *rtf_ux, double *const *grad_out) override
+    {
+        (void)ishot;
+        const psv_grid &g = sv.g;
+        const int nz = g.nz, nx = g.nx;
+        const size_t n = (size_t)nz * nx;
+        PSV_CU(cudaMemcpyAsync(lam(), l, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(mu(), m, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(avg(0), mzx, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(avg(1), rzp, n * 8, cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(avg(2), rxp, n * 8, cudaMemcpyHostToDevice, st));
+        double rzmax = 0.0;
+        for (size_t k = 0; k < n; k++) rzmax = std::max(rzmax, std::max(std::fabs(rzp[k]), std::fabs(rxp[k])));
+        model_scales(l, m, rzmax > 0 ? rzmax : 1.0);
+        double sc = 1.0;  // amplitude scale of this call's wavefields
+        PSV_CU(cudaMemcpy(&sc, fscale(), 8, cudaMemcpyDeviceToHost));
+        if (grad_) {  // adjoint sources are the caller's: same rule as the forward gain
+            const double h2[2] = {sc, 1.0 / sc};
+            PSV_CU(cudaMemcpy(ascale(), h2, 8, cudaMemcpyHostToDevice));
+            qk.amp_scale = ascale();
+        }
+        PSV_TRY(coefficients(false, true));
+        PSV_TRY(set_batch(0));
+        const long long snp = sp.snap_plane;
+        const double un = 1.0 / sc;
+        if (grad_ || accu) PSV_TRY(ensure_hist());
+        if (grad_) {  // forward history in (gard_fwd_storage2 layout [snap_nt][snap_nz][snap_nx])
+            std::vector<T> h((size_t)hist_shot, T(0));
+            const int map[5] = {H_VZ, H_VX, H_SZZ, H_SZX, H_SXX};
+            for (int k = 0; k < 5; k++)
+                for (int t = 0; t < sv.snt; t++)
+                    for (int jz = 0; jz < sv.snz; jz++)
+                        for (int jx = 0; jx < sv.snx; jx++)
+                            h[(size_t)t * NHIST * snp + map[k] * snp + (size_t)jz * snx_pitch + jx] =
+                                (T)accu_io[k][((size_t)t * sv.snz + jz) * sv.snx + jx];
+            PSV_CU(cudaMemcpyAsync(hist.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+            PSV_CU(cudaStreamSynchronize(st));
+            PSV_TRY(run_pass(PASS_ADJ_GIVEN));
+        } else {
+            store_flag = accu != 0;
+            PSV_TRY(run_pass(PASS_FWD_U));
+            store_flag = false;
+        }
+        PSV_CU(cudaStreamSynchronize(st));
+        // wavefields: vz vx uz ux szz szx sxx We
+        std::vector<T> pl((size_t)shot_stride);
+        PSV_CU(cudaMemcpy(pl.data(), fld.p, pl.size() * sizeof(T), cudaMemcpyDeviceToHost));
+        const int fmap[8] = {F_VZ, F_VX, F_UZ, F_UX, F_SZZ, F_SZX, F_SXX, grad_ ? F_WEA : F_WE};
+        for (int k = 0; k < 8; k++)
+            if (fields_out[k])
+                for (int iz = 0; iz < nz; iz++)
+                    for (int ix = 0; ix < nx; ix++)
+                        fields_out[k][(size_t)iz * nx + ix] =
+                            (double)pl[fmap[k] * plane + (size_t)iz * pitch + ix] * (k == 7 ? un * un : un);
+        // CPML memories: mem_vz_z mem_vx_z mem_szz_z mem_szx_z mem_vz_x mem_vx_x mem_szx_x mem_sxx_x
+        std::vector<T> mz((size_t)std::max<long long>(mz_shot, 1)), mxv((size_t)std::max<long long>(mx_shot, 1));
+        if (mz_shot) PSV_CU(cudaMemcpy(mz.data(), memz.p, mz_shot * sizeof(T), cudaMemcpyDeviceToHost));
+        if (mx_shot) PSV_CU(cudaMemcpy(mxv.data(), memx.p, mx_shot * sizeof(T), cudaMemcpyDeviceToHost));
+        for (int k = 0; k < 8; k++) {
+            if (!mem_out[k]) continue;
+            std::fill(mem_out[k], mem_out[k] + n, 0.0);
+            for (int iz = 0; iz < nz; iz++)
+                for (int ix = 0; ix < nx; ix++) {
+                    if (k < 4 && nzs && (iz < sv.pz0 || iz >= sv.pz1)) {
+                        const int r = iz < sv.pz0 ? iz : iz - sv.pz1 + sv.pz0;
+                        mem_out[k][(size_t)iz * nx + ix] = (double)mz[(size_t)k * nzs * pitch + (size_t)r * pitch + ix] * un;
+                    } else if (k >= 4 && nxs && (ix < sv.px0 || ix >= sv.px1)) {
+                        const int c = ix < sv.px0 ? ix : ix - sv.px1 + sv.px0;
+                        mem_out[k][(size_t)iz * nx + ix] =
+                            (double)mxv[(size_t)(k - 4) * nz * mx_pitch + (size_t)iz * mx_pitch + c] * un;
+                    }
+                }
+        }
+        const int nrec = sv.s.nrec, nt = g.nt;
+        if (!grad_ && nrec && (rtf_uz || rtf_ux)) {
+            std::vector<double> a((size_t)ntr), b((size_t)ntr);
+            PSV_CU(cudaMemcpy(a.data(), tr(0), ntr * 8, cudaMemcpyDeviceToHost));
+            PSV_CU(cudaMemcpy(b.data(), tr(1), ntr * 8, cudaMemcpyDeviceToHost));
+            for (int r = 0; r < nrec; r++)
+                for (int t = 0; t < nt; t++) {
+                    if (rtf_uz) rtf_uz[(size_t)r * nt + t] = a[(size_t)t * nrec + r];
+                    if (rtf_ux) rtf_ux[(size_t)r * nt + t] = b[(size_t)t * nrec + r];
+                }
+        }
+        if (!grad_ && accu) {
+            std::vector<T> h((size_t)hist_shot);
+            PSV_CU(cudaMemcpy(h.data(), hist.p, h.size() * sizeof(T), cudaMemcpyDeviceToHost));
+            const int map[5] = {H_VZ, H_VX, H_SZZ, H_SZX, H_SXX};
+            for (int k = 0; k < 5; k++)
+                if (accu_io[k])
+                    for (int t = 0; t < sv.snt; t++)
+                        for (int jz = 0; jz < sv.snz; jz++)
+                            for (int jx = 0; jx < sv.snx; jx++)
+                                accu_io[k][((size_t)t * sv.snz + jz) * sv.snx + jx] =
+                                    (double)h[(size_t)t * NHIST * snp + map[k] * snp + (size_t)jz * snx_pitch + jx] * un;
+        }
+        if (grad_) {
+            std::vector<T> h((size_t)gshot_shot);
+            PSV_CU(cudaMemcpy(h.data(), gshot.p, h.size() * sizeof(T), cudaMemcpyDeviceToHost));
+            for (int k = 0; k < 3; k++)
+                if (grad_out[k])
+                    for (int jz = 0; jz < sv.snz; jz++)
+                        for (int jx = 0; jx < sv.snx; jx++)
+                            grad_out[k][(size_t)jz * sv.snx + jx] =
+                                (double)h[k * snp + (size_t)jz * snx_pitch + jx] * (k < 2 ? un / gscale : un) *
+                                (g.imaging_sign > 0 ? -1.0 : 1.0);
+        }
+        return PSV_OK;
+    }
+};
+
+template <typename T>
+std::unique_ptr<PlanIface> make_plan_t(const Survey &sv, const psv_options &opt, int &status)
+{
+    std::unique_ptr<Plan<T>> p(new Plan<T>());
+    status = p->init(sv, opt);
+    if (status != PSV_OK) return nullptr;
+    return std::unique_ptr<PlanIface>(p.release());
+}
+
+}  // namespace psv

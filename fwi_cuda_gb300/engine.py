@@ -1,0 +1,213 @@
+"""Python front-end of the GB300 engine (thin wrapper over the C ABI).
+
+* :class:`Plan` -- a device-resident survey: forward modelling, FWI gradient,
+  FWI iteration with the reference's step-length search
+  (``simulate_fwd_PSV`` / ``simulate_fwi_PSV``, include/cpu/n_simulate_PSV.hpp).
+* :func:`kernel_PSV` -- the reference's per-shot time loop (``kernel_PSV``,
+  include/cpu/n_kernel_PSV.hpp:8-43) with the same argument meaning.
+* :func:`simulate_PSV` -- the reference's whole program on the GPU
+  (``simulate_PSV``, include/h_simulate_PSV.hpp:23).
+
+Every call goes to ``libfwi_psv.so``; nothing here computes on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import PsvOptions, check, dptr, f64, i32, iptr
+
+
+def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
+            block=(0, 0), checkpoint_interval=0) -> PsvOptions:
+    o = PsvOptions()
+    _lib.lib().psv_options_default(C.byref(o))
+    o.precision = int(precision)
+    o.storage = _lib.STORAGE[storage]
+    o.hbm_budget_gb = float(hbm_budget_gb)
+    o.max_batch = int(max_batch)
+    o.use_graphs = int(bool(use_graphs))
+    o.block_x, o.block_y = int(block[0]), int(block[1])
+    o.checkpoint_interval = int(checkpoint_interval)
+    return o
+
+
+class Plan:
+    def __init__(self, survey, **opts):
+        self.sv = survey
+        self._keep = []
+        g = survey.grid_struct(self._keep)
+        s = survey.shots_struct(self._keep)
+        o = options(**opts)
+        h = C.c_void_p()
+        check(_lib.lib().psv_plan_create(C.byref(g), C.byref(s), C.byref(o), C.byref(h)))
+        self.h = h
+        self.n = survey.nz * survey.nx
+
+    def close(self):
+        if getattr(self, "h", None):
+            _lib.lib().psv_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def device_bytes(self) -> int:
+        return int(_lib.lib().psv_plan_device_bytes(self.h))
+
+    def set_model(self, lam, mu, rho):
+        self._model = [f64(lam), f64(mu), f64(rho)]
+        check(_lib.lib().psv_plan_set_model(self.h, *[dptr(a) for a in self._model]))
+
+    def get_model(self):
+        out = [np.zeros((self.sv.nz, self.sv.nx)) for _ in range(3)]
+        check(_lib.lib().psv_plan_get_model(self.h, *[dptr(a) for a in out]))
+        return out
+
+    def set_observed(self, uz, ux):
+        self._obs = [f64(uz), f64(ux)]
+        check(_lib.lib().psv_plan_set_observed(self.h, dptr(self._obs[0]), dptr(self._obs[1])))
+
+    def forward(self):
+        sv = self.sv
+        uz = np.zeros((sv.nshot, sv.nrec, sv.nt))
+        ux = np.zeros_like(uz)
+        check(_lib.lib().psv_forward(self.h, dptr(uz), dptr(ux)))
+        return uz, ux
+
+    def gradient(self, fetch=True):
+        L2 = C.c_double()
+        if fetch:
+            g = [np.zeros((self.sv.nz, self.sv.nx)) for _ in range(3)]
+            check(_lib.lib().psv_gradient(self.h, C.byref(L2), *[dptr(a) for a in g]))
+            return L2.value, g
+        check(_lib.lib().psv_gradient(self.h, C.byref(L2), None, None, None))
+        return L2.value, None
+
+    def reset_gradient(self):
+        check(_lib.lib().psv_reset_gradient(self.h))
+
+    def get_gradient(self):
+        g = [np.zeros((self.sv.nz, self.sv.nx)) for _ in range(3)]
+        check(_lib.lib().psv_get_gradient(self.h, *[dptr(a) for a in g]))
+        return g
+
+    def set_gradient(self, gl, gm, gr):
+        arrs = [f64(gl), f64(gm), f64(gr)]
+        check(_lib.lib().psv_set_gradient(self.h, *[dptr(a) for a in arrs]))
+
+    def shot_gradient(self, ishot):
+        sv = self.sv
+        snt, snz, snx = sv.snap_dims()
+        out = {k: np.zeros((snz, snx)) for k in ("grad_lam", "grad_mu", "grad_rho")}
+        out["We"] = np.zeros((sv.nz, sv.nx))
+        out["We_adj"] = np.zeros((sv.nz, sv.nx))
+        out["rtf_uz"] = np.zeros((sv.nrec, sv.nt))
+        out["rtf_ux"] = np.zeros((sv.nrec, sv.nt))
+        L2 = C.c_double()
+        check(_lib.lib().psv_get_shot_gradient(
+            self.h, ishot, dptr(out["grad_lam"]), dptr(out["grad_mu"]), dptr(out["grad_rho"]),
+            dptr(out["We"]), dptr(out["We_adj"]), dptr(out["rtf_uz"]), dptr(out["rtf_ux"]),
+            C.byref(L2)))
+        out["L2"] = L2.value
+        return out
+
+    def fwi_iteration(self, step, max_trials=64):
+        st = C.c_double(step)
+        L2 = C.c_double()
+        nt = C.c_int()
+        tlog = np.zeros((max_trials, 2))
+        check(_lib.lib().psv_fwi_iteration(self.h, C.byref(st), C.byref(L2), C.byref(nt),
+                                           dptr(tlog), max_trials))
+        n = nt.value
+        return dict(step=st.value, L2=L2.value, ntrials=n, trials=tlog[:min(n, max_trials)].copy())
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the plan (for torch.cuda.ExternalStream)."""
+        return int(_lib.lib().psv_plan_stream(self.h) or 0)
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(_lib.lib().psv_plan_kernel_launches(self.h))
+
+    def profile_kernels(self, nsteps=100):
+        ms = np.zeros(6)
+        check(_lib.lib().psv_profile_kernels(self.h, int(nsteps), dptr(ms)))
+        return dict(stress_fwd=ms[0], velocity_fwd=ms[1], srcrec_fwd=ms[2],
+                    stress_adj=ms[3], velocity_adj=ms[4], srcrec_adj=ms[5])
+
+    def timing(self):
+        t = np.zeros(3)
+        check(_lib.lib().psv_last_timing(self.h, dptr(t)))
+        return dict(forward_ms=t[0], adjoint_ms=t[1], other_ms=t[2])
+
+
+def kernel_PSV(ishot, nt, nz, nx, dt, dx, dz, surf, isurf, hc, fdorder, lam, mu, mu_zx, rho_zp,
+               rho_xp, grad, pml_z, cpml_z, pml_x, cpml_x, nsrc, stf_type, stf_z, stf_x, z_src,
+               x_src, src_shot_to_fire, nrec, rtf_type, z_rec, x_rec, accu, snap, history=None,
+               stencil="reference", precision=32):
+    """One shot, nt steps, forward (grad=False) or time-reversed adjoint
+    (grad=True), arguments as the reference's kernel_PSV.  ``cpml_z`` /
+    ``cpml_x`` are the six profiles (a, b, K, a_half, b_half, K_half);
+    ``snap`` = (snap_z1, snap_z2, snap_x1, snap_x2, snap_dt, snap_dz, snap_dx);
+    ``history`` = the forward snapshots {vz, vx, szz, szx, sxx} (adjoint).
+    Returns every array the reference leaves filled."""
+    n = (nz, nx)
+    f = {k: np.zeros(n) for k in ("vz", "vx", "uz", "ux", "szz", "szx", "sxx", "We")}
+    mem = {k: np.zeros(n) for k in ("mem_vz_z", "mem_vx_z", "mem_szz_z", "mem_szx_z",
+                                    "mem_vz_x", "mem_vx_x", "mem_szx_x", "mem_sxx_x")}
+    z1, z2, x1, x2, sdt, sdz, sdx = snap
+    snt, snz, snx = 1 + (nt - 1) // sdt, 1 + (z2 - z1) // sdz, 1 + (x2 - x1) // sdx
+    gr = {k: np.zeros((snz, snx)) for k in ("grad_lam", "grad_mu", "grad_rho")}
+    hist = {}
+    for k in ("vz", "vx", "szz", "szx", "sxx"):
+        if history is not None:
+            hist[k] = f64(history[k]).copy()
+        else:
+            hist[k] = np.zeros((snt, snz, snx) if accu else (1,))
+    rtf_uz = np.zeros((max(nrec, 1), nt))
+    rtf_ux = np.zeros_like(rtf_uz)
+    keep = [f64(a) for a in (lam, mu, mu_zx, rho_zp, rho_xp)]
+    cz = [f64(a) for a in cpml_z] if pml_z else [np.ones(nz)] * 6
+    cx = [f64(a) for a in cpml_x] if pml_x else [np.ones(nx)] * 6
+    src = [f64(stf_z), f64(stf_x), i32(z_src), i32(x_src), i32(src_shot_to_fire)]
+    rec = [i32(z_rec), i32(x_rec)]
+    isurf_a = i32(isurf if isurf is not None else [0, 0, 0, 0])
+    hc_a = f64(hc)
+    args = [ishot, nt, nz, nx, dt, dx, dz, int(surf), iptr(isurf_a), dptr(hc_a), fdorder]
+    args += [dptr(f[k]) for k in ("vz", "vx", "uz", "ux", "szz", "szx", "sxx", "We")]
+    args += [None] * 4
+    args += [dptr(a) for a in keep]
+    args += [int(grad)] + [dptr(gr[k]) for k in ("grad_lam", "grad_mu", "grad_rho")]
+    args += [int(pml_z)] + [dptr(a) for a in cz] + [int(pml_x)] + [dptr(a) for a in cx]
+    args += [dptr(mem[k]) for k in mem]
+    args += [nsrc, stf_type, dptr(src[0]), dptr(src[1]), iptr(src[2]), iptr(src[3]), iptr(src[4])]
+    args += [nrec, rtf_type, dptr(rtf_uz), dptr(rtf_ux), iptr(rec[0]), iptr(rec[1])]
+    args += [int(accu)] + [dptr(hist[k]) for k in ("vz", "vx", "szz", "szx", "sxx")]
+    args += [z1, z2, x1, x2, sdt, sdz, sdx, _lib.STENCIL[stencil], int(precision)]
+    check(_lib.lib().psv_kernel_PSV(*args))
+    out = dict(f)
+    out.update(mem)
+    out.update(gr)
+    out["rtf_uz"], out["rtf_ux"] = rtf_uz[:nrec], rtf_ux[:nrec]
+    out["history"] = hist
+    return out
+
+
+def simulate_PSV(workdir: str, max_iter: int = 0, **opts) -> None:
+    """Run the reference's program (inputs under workdir/bin, workdir/io) on the GPU."""
+    o = options(**opts)
+    check(_lib.lib().psv_simulate_PSV(workdir.encode(), int(max_iter), C.byref(o)))

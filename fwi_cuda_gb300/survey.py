@@ -1,0 +1,264 @@
+"""Survey description and seeded synthetic models.
+
+A :class:`Survey` holds what the reference reads from its binary inputs
+(``scripts/pre_proc_fwi.py:240-276`` / ``src/h_simulate_PSV.cpp:99-185``):
+grid, CPML parameters, snapshot window, taper, sources and receivers.
+:meth:`Survey.finalize` derives the Holberg coefficients and the CPML
+profiles with the engine's host functions (``psv_holbergcoeff``,
+``psv_cpml_PSV``), exactly as ``simulate_PSV`` does.
+
+The generators below build the layered-plus-anomaly models of the
+benchmark configurations from a seed (no dataset is involved): horizontal
+or dipping layers with vp drawn uniformly and sorted with depth,
+vs = vp / 1.73, Gardner density rho = 310 vp^0.25, Gaussian vp anomalies.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import PsvGrid, PsvShots, dptr, f64, i32, iptr
+
+
+def ricker(nt: int, dt: float, fc: float, amp: float = 1.0, ts: float = 0.0) -> np.ndarray:
+    """Ricker wavelet of the reference (wavelet, src/h_preproc_PSV.cpp:267-286)."""
+    s = np.zeros(nt)
+    _lib.check(_lib.lib().psv_wavelet(dptr(s), nt, dt, amp, fc, ts, 1))
+    return s
+
+
+def holbergcoeff(fdorder: int, maxrelerror: int = 1) -> np.ndarray:
+    hc = np.zeros(7)
+    _lib.check(_lib.lib().psv_holbergcoeff(fdorder, maxrelerror, dptr(hc)))
+    return hc
+
+
+def cpml_profiles(npower, damp, rcoef, kmax, freq, n1, n2, fpad, nh, dt, dh):
+    arrs = [np.zeros(nh) for _ in range(6)]
+    _lib.check(_lib.lib().psv_cpml_PSV(*[dptr(a) for a in arrs], npower, damp, rcoef, kmax, freq,
+                                       n1, n2, fpad, nh, dt, dh))
+    return arrs
+
+
+@dataclass
+class Survey:
+    nt: int
+    nz: int
+    nx: int
+    dt: float
+    dz: float
+    dx: float
+    fdorder: int = 4
+    stencil: str = "reference"       # "reference" (2-point x hc[1]) or "holberg"
+    npml: tuple = (0, 20, 20, 20)    # top, bottom, left, right
+    fpad: int | None = None          # CPML padding (metaint's fpad); default fdorder // 2
+    surf: bool = False
+    isurf: tuple = (0, 0, 0, 0)
+    npower: float = 2.0
+    damp_v_pml: float = 3000.0
+    rcoef: float = 0.001
+    k_max_pml: float = 1.0
+    freq_pml: float = 100.0
+    snap_z1: int = 0
+    snap_z2: int = 0
+    snap_x1: int = 0
+    snap_x2: int = 0
+    snap_dt: int = 1
+    snap_dz: int = 1
+    snap_dx: int = 1
+    taper: tuple = (0, 0, 0, 0, 0, 0, 0, 0)
+    imaging_sign: int = -1           # -1: reference CPU path (grad -=); +1: its CUDA path (+=)
+    nshot: int = 1
+    stf_type: int = 0
+    rtf_type: int = 0
+    z_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    x_src: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    src_shot_to_fire: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    stf_z: np.ndarray = field(default_factory=lambda: np.zeros((0, 0)))
+    stf_x: np.ndarray = field(default_factory=lambda: np.zeros((0, 0)))
+    z_rec: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    x_rec: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+
+    def finalize(self) -> "Survey":
+        """Holberg coefficients and CPML profiles (h_simulate_PSV.cpp:155-170)."""
+        if self.fpad is None:
+            self.fpad = self.fdorder // 2
+        self.hc = holbergcoeff(self.fdorder, 1)
+        self.pml_z = bool(self.npml[0] or self.npml[1])
+        self.pml_x = bool(self.npml[2] or self.npml[3])
+        z = cpml_profiles(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
+                          self.npml[0], self.npml[1], self.fpad, self.nz, self.dt, self.dz)
+        x = cpml_profiles(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
+                          self.npml[2], self.npml[3], self.fpad, self.nx, self.dt, self.dx)
+        (self.a_z, self.b_z, self.K_z, self.a_half_z, self.b_half_z, self.K_half_z) = z
+        (self.a_x, self.b_x, self.K_x, self.a_half_x, self.b_half_x, self.K_half_x) = x
+        self.z_src, self.x_src = i32(self.z_src), i32(self.x_src)
+        self.src_shot_to_fire = i32(self.src_shot_to_fire)
+        self.z_rec, self.x_rec = i32(self.z_rec), i32(self.x_rec)
+        self.stf_z = f64(self.stf_z).reshape(len(self.z_src), self.nt)
+        self.stf_x = f64(self.stf_x).reshape(len(self.z_src), self.nt)
+        return self
+
+    @property
+    def nsrc(self) -> int:
+        return int(len(self.z_src))
+
+    @property
+    def nrec(self) -> int:
+        return int(len(self.z_rec))
+
+    def snap_dims(self):
+        return (1 + (self.nt - 1) // self.snap_dt,
+                1 + (self.snap_z2 - self.snap_z1) // self.snap_dz,
+                1 + (self.snap_x2 - self.snap_x1) // self.snap_dx)
+
+    def grid_struct(self, keep: list) -> PsvGrid:
+        g = PsvGrid()
+        g.nt, g.nz, g.nx = self.nt, self.nz, self.nx
+        g.dt, g.dx, g.dz = self.dt, self.dx, self.dz
+        g.fdorder = self.fdorder
+        g.stencil = _lib.STENCIL[self.stencil]
+        g.surf = int(self.surf)
+        for i in range(4):
+            g.isurf[i] = int(self.isurf[i])
+        for i in range(7):
+            g.hc[i] = float(self.hc[i])
+        g.pml_z, g.pml_x = int(self.pml_z), int(self.pml_x)
+        for name in ("a_z", "b_z", "K_z", "a_half_z", "b_half_z", "K_half_z",
+                     "a_x", "b_x", "K_x", "a_half_x", "b_half_x", "K_half_x"):
+            a = f64(getattr(self, name))
+            keep.append(a)
+            setattr(g, name, dptr(a))
+        (g.snap_z1, g.snap_z2, g.snap_x1, g.snap_x2, g.snap_dt, g.snap_dz, g.snap_dx) = (
+            self.snap_z1, self.snap_z2, self.snap_x1, self.snap_x2, self.snap_dt, self.snap_dz,
+            self.snap_dx)
+        for i in range(8):
+            g.taper[i] = int(self.taper[i])
+        g.imaging_sign = int(self.imaging_sign)
+        return g
+
+    def shots_struct(self, keep: list) -> PsvShots:
+        s = PsvShots()
+        s.nshot, s.nsrc, s.nrec = self.nshot, self.nsrc, self.nrec
+        s.stf_type, s.rtf_type = self.stf_type, self.rtf_type
+        arrs = dict(z_src=i32(self.z_src), x_src=i32(self.x_src),
+                    src_shot_to_fire=i32(self.src_shot_to_fire), z_rec=i32(self.z_rec),
+                    x_rec=i32(self.x_rec), stf_z=f64(self.stf_z), stf_x=f64(self.stf_x))
+        keep.extend(arrs.values())
+        for k, v in arrs.items():
+            setattr(s, k, iptr(v) if v.dtype == np.int32 else dptr(v))
+        return s
+
+
+# ----------------------------------------------------------------------------
+# Seeded synthetic models
+# ----------------------------------------------------------------------------
+
+def elastic_from_velocity(vp, vs, rho):
+    """lam, mu from velocities (Pa): mu = rho vs^2, lam = rho vp^2 - 2 mu."""
+    mu = rho * vs * vs
+    lam = rho * vp * vp - 2.0 * mu
+    return f64(lam), f64(mu), f64(rho)
+
+
+def layered_vp(nz, nx, n_layers, vp_lo, vp_hi, rng, dip_cells=0.0, top=0, fault=None):
+    """Layers with vp ~ U[vp_lo, vp_hi] sorted increasing with depth.
+
+    dip_cells: depth change of each interface across the model (cells).
+    fault: (x_index, throw_cells) shifts the interfaces right of x_index.
+    """
+    vps = np.sort(rng.uniform(vp_lo, vp_hi, n_layers))
+    cuts = np.sort(rng.uniform(0.15, 0.9, n_layers - 1)) * (nz - top) + top
+    iz = np.arange(nz)[:, None].astype(np.float64)
+    ix = np.arange(nx)[None, :].astype(np.float64)
+    vp = np.full((nz, nx), vps[0])
+    for k in range(n_layers - 1):
+        depth = cuts[k] + dip_cells * (ix / max(nx - 1, 1) - 0.5)
+        if fault is not None:
+            depth = depth + np.where(ix >= fault[0], fault[1], 0.0)
+        vp = np.where(iz >= depth, vps[k + 1], vp)
+    return vp
+
+
+def add_anomalies(vp, rng, n, amp=0.10, radius=(15, 15), signs=(1,), margin=0):
+    nz, nx = vp.shape
+    iz = np.arange(nz)[:, None]
+    ix = np.arange(nx)[None, :]
+    out = vp.copy()
+    for _ in range(n):
+        r = rng.uniform(radius[0], radius[1])
+        cz = rng.uniform(margin + r, nz - margin - r)
+        cx = rng.uniform(margin + r, nx - margin - r)
+        sgn = signs[int(rng.integers(len(signs)))]
+        out = out * (1.0 + sgn * amp * np.exp(-((iz - cz) ** 2 + (ix - cx) ** 2) / (r * r)))
+    return out
+
+
+def model_from_vp(vp, vs_ratio=1.73):
+    vs = vp / vs_ratio
+    rho = 310.0 * vp ** 0.25
+    return elastic_from_velocity(vp, vs, rho)
+
+
+def smoothed(vp, sigma, vs_ratio=1.73):
+    from scipy.ndimage import gaussian_filter
+    return model_from_vp(gaussian_filter(vp, sigma, mode="nearest"), vs_ratio)
+
+
+def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml=20, nshot=1,
+                   nrec=120, rec_spacing=4, src_depth=4, rec_depth=2, fc=100.0, vp_max=3000.0,
+                   snap_dt=1, surf_offset=None, force="z", seed=0) -> Survey:
+    """Free surface on top, CPML on the other three sides, shots evenly
+    spread along the surface, receivers on a line below the surface."""
+    fpad = fdorder // 2
+    isurf = fpad + (surf_offset if surf_offset is not None else fpad)
+    span = rec_spacing * (nrec - 1)
+    x0 = (nx - 1 - span) // 2
+    x_rec = x0 + rec_spacing * np.arange(nrec)
+    if nshot == 1:
+        x_src = np.array([(nx - 1) // 2])
+    else:
+        x_src = np.linspace(x_rec[0] if nrec else npml + fpad + 4,
+                            x_rec[-1] if nrec else nx - npml - fpad - 5, nshot).round()
+    w = ricker(nt, dt, fc)
+    stf = np.stack([w] * nshot)
+    zero = np.zeros_like(stf)
+    snap_z1, snap_z2 = fpad, nz - fpad - 1
+    snap_x1, snap_x2 = fpad, nx - fpad - 1
+    t = max(1, npml // 2)
+    taper = (isurf + 1, isurf + 1 + t, nz - npml - fpad - 1, nz - npml - fpad - 1 - t,
+             npml + fpad + 1, npml + fpad + 1 + t, nx - npml - fpad - 1, nx - npml - fpad - 1 - t)
+    sv = Survey(nt=nt, nz=nz, nx=nx, dt=dt, dz=dz, dx=dx, fdorder=fdorder, stencil=stencil,
+                npml=(0, npml, npml, npml), surf=True, isurf=(isurf, 0, 0, 0),
+                damp_v_pml=vp_max, freq_pml=fc,
+                snap_z1=snap_z1, snap_z2=snap_z2, snap_x1=snap_x1, snap_x2=snap_x2,
+                snap_dt=snap_dt, taper=taper, nshot=nshot, stf_type=0, rtf_type=0,
+                z_src=np.full(nshot, isurf + src_depth), x_src=x_src.astype(np.int32),
+                src_shot_to_fire=np.arange(nshot), stf_z=stf if force == "z" else zero,
+                stf_x=zero if force == "z" else stf,
+                z_rec=np.full(nrec, isurf + rec_depth), x_rec=x_rec)
+    return sv.finalize()
+
+
+def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
+                   stencil="holberg", npml=20, nrec=120, seed=1234, snap_dt=1, n_layers=5,
+                   vp_range=(1800.0, 3000.0), anomaly_radius=15, smooth_sigma=15.0, fc=100.0):
+    """The 301 x 601 layered-plus-anomaly survey (one shot: forward + one
+    adjoint gradient; eight shots: the FWI iteration case).  Smaller sizes
+    give the same structure for tests.  Returns (survey, true model, initial
+    model) with models as (lam, mu, rho)."""
+    rng = np.random.default_rng(seed)
+    fpad = fdorder // 2
+    vp = layered_vp(nz, nx, n_layers, *vp_range, rng, top=2 * fpad)
+    vp = add_anomalies(vp, rng, 1, amp=0.10, radius=(anomaly_radius, anomaly_radius),
+                       margin=npml + fpad)
+    true = model_from_vp(vp)
+    init = smoothed(vp, smooth_sigma)
+    rec_spacing = max(1, min(4, (nx - 2 * (npml + fpad) - 8) // max(nrec - 1, 1)))
+    sv = surface_survey(nz, nx, dx, dx, nt, dt, fdorder=fdorder, stencil=stencil, npml=npml,
+                        nshot=nshot, nrec=nrec, rec_spacing=rec_spacing, fc=fc,
+                        vp_max=float(vp.max()), snap_dt=snap_dt, seed=seed)
+    return sv, true, init

@@ -1,0 +1,271 @@
+/*
+ * fwi_psv.h -- C ABI of the GB300 P/SV finite-difference engine.
+ *
+ * The engine replaces the time loop of Mohammad-debug/FWI_CUDA (kernel_PSV,
+ * include/cpu/n_kernel_PSV.hpp:8-43, and its CUDA twin kernel_PSV_GPU,
+ * include/cuda/d_kernel_PSV.cuh:9-44) and the shot/FWI drivers that call it
+ * (simulate_fwd_PSV / simulate_fwi_PSV, include/cpu/n_simulate_PSV.hpp:23-44;
+ * step_length_PSV, include/cpu/n_step_length_PSV.hpp:17).  Wavefields live on
+ * one GB300 in FP32 (or FP64 on request); every array crossing this boundary
+ * is a caller-owned HOST array in FP64 with the reference's row-major layout:
+ *   field          [nz][nx]
+ *   time function  [n][nt]           (stf, one shot's seismograms)
+ *   survey traces  [nshot][nrec][nt]  (rtf_*_true, allocate_array(...,nshot,nrec,nt))
+ *   snapshot       [snap_nt][snap_nz][snap_nx]
+ *
+ * Conventions (the reference prints and calls exit(0) on errors,
+ * include/cuda/d_globvar.cuh:23-29; this ABI never exits):
+ *   - every function returns a psv_status; psv_last_error() gives the text;
+ *   - no host memory is retained after a call returns;
+ *   - a plan is used by one host thread at a time; plans are independent;
+ *   - there is no CPU fallback: without a usable GPU calls return
+ *     PSV_ERR_CUDA.
+ */
+#ifndef FWI_PSV_H
+#define FWI_PSV_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    PSV_OK = 0,
+    PSV_ERR_ARG = 1,          /* invalid or inconsistent argument */
+    PSV_ERR_CFL = 2,          /* time step above the stability limit */
+    PSV_ERR_OOM = 3,          /* device memory or HBM budget exceeded */
+    PSV_ERR_CUDA = 4,         /* CUDA runtime error / no device */
+    PSV_ERR_UNSUPPORTED = 5,  /* valid for the reference, not implemented here */
+    PSV_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+    PSV_ERR_STEP_SEARCH = 7,  /* step-length search failed (reference: exit(0)) */
+    PSV_ERR_IO = 8            /* file missing / short read / write failed */
+} psv_status;
+
+#define PSV_STENCIL_REFERENCE 0 /* reference: 2-point difference x hc[1], pad fdorder/2 */
+#define PSV_STENCIL_HOLBERG 1   /* full 2N-point staggered Holberg stencil, N = fdorder/2 */
+
+#define PSV_STORE_AUTO 0        /* full history when it fits the budget, else checkpoints */
+#define PSV_STORE_FULL 1        /* every snapshot kept in HBM (the reference's accu_*) */
+#define PSV_STORE_CHECKPOINT 2  /* checkpoints + recomputation of the forward */
+
+const char *psv_error_string(int status);
+/* Message of the last failing call on this host thread. */
+const char *psv_last_error(void);
+/* 1 when a CUDA device is usable, else 0. */
+int psv_device_available(void);
+
+/* ------------------------------------------------------------------------ */
+/* Host preprocessing (FP64, bitwise equal to the reference's formulas).     */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces holbergcoeff, include/h_holbergcoeff.hpp:23 (hc7 has 7 entries). */
+int psv_holbergcoeff(int fdorder, int maxrelerror, double *hc7);
+
+/* Replaces cpml_PSV, include/h_preproc_PSV.hpp:41-44 (arrays of length nh). */
+int psv_cpml_PSV(double *a, double *b, double *K, double *a_half, double *b_half,
+                 double *K_half, double npower, double damp_v_PML, double rcoef,
+                 double k_max_PML, double freq, int npml_h1, int npml_h2, int fpad, int nh,
+                 double dt, double dh);
+
+/* Replaces wavelet, include/h_preproc_PSV.hpp:48 (shape 1 = Ricker). */
+int psv_wavelet(double *signal, int nt, double dt, double amp, double fc, double ts, int shape);
+
+/* Replaces checkfd_ssg_elastic, include/h_checkfd_ssg_elastic.hpp:16.
+ * out4 = {dtstab, dhstab, cmax, cmin}.  Returns PSV_ERR_CFL when dt > dtstab,
+ * PSV_ERR_ARG when the absorbing frame fw exceeds the domain (where the
+ * reference exits), else PSV_OK. */
+int psv_checkfd_ssg_elastic(int nz, int nx, double dh, double dt, double ts, int fw,
+                            const double *rho, const double *lam, const double *mu,
+                            const double *hc7, double *out4);
+
+/* ------------------------------------------------------------------------ */
+/* Survey description                                                         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct psv_grid {
+    int nt, nz, nx;
+    double dt, dx, dz;
+    int fdorder;         /* 2, 4, 6 or 8 */
+    int stencil;         /* PSV_STENCIL_* */
+    int surf;            /* free surface present */
+    int isurf[4];        /* 0 top, 1 bottom, 2 left, 3 right; 0 = none */
+    double hc[7];        /* psv_holbergcoeff output */
+    int pml_z, pml_x;
+    /* CPML profiles (psv_cpml_PSV output): [nz] for *_z, [nx] for *_x.
+     * Ignored (may be NULL) when the axis has no PML. */
+    const double *a_z, *b_z, *K_z, *a_half_z, *b_half_z, *K_half_z;
+    const double *a_x, *b_x, *K_x, *a_half_x, *b_half_x, *K_half_x;
+    /* Snapshot / gradient window, inclusive, and subsampling. */
+    int snap_z1, snap_z2, snap_x1, snap_x2, snap_dt, snap_dz, snap_dx;
+    /* Tukey taper of the gradient: t1 t2 b1 b2 l1 l2 r1 r2 (taper2). */
+    int taper[8];
+    /* Sign of the imaging condition.  <= 0: the reference's CPU path,
+     * grad -= ... (src/cpu/n_kernel_lib_PSV.cpp:477-479); > 0: its CUDA path,
+     * grad += ... (src/cuda/d_kernel_lib_PSV.cu:838-840).  The two differ by
+     * an exact negation of every gradient. */
+    int imaging_sign;
+} psv_grid;
+
+typedef struct psv_shots {
+    int nshot, nsrc, nrec;
+    int stf_type;                /* 0 displacement, 1 velocity (vsrc2) */
+    int rtf_type;                /* 0 displacement (urec2) */
+    const int *z_src, *x_src;    /* [nsrc] grid indices */
+    const int *src_shot_to_fire; /* [nsrc] shot index that fires each source */
+    const double *stf_z, *stf_x; /* [nsrc][nt] */
+    const int *z_rec, *x_rec;    /* [nrec] */
+} psv_shots;
+
+typedef struct psv_options {
+    int precision;              /* 32 (default) or 64 */
+    int storage;                /* PSV_STORE_* */
+    double hbm_budget_gb;       /* device memory the plan may use; 0 = 180 */
+    int checkpoint_interval;    /* CHECKPOINT storage: steps per segment, 0 = auto */
+    int max_batch;              /* shots per launch; 0 = all shots of the survey */
+    int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
+    int block_x, block_y;       /* thread-block shape of the stencil kernels; 0 = tuned */
+} psv_options;
+
+void psv_options_default(psv_options *opt);
+
+typedef struct psv_plan psv_plan;
+
+/* Allocates the device state of a survey (wavefields of max_batch shots,
+ * snapshot storage or checkpoints, materials, traces).  The grid/shots
+ * arrays are copied; the caller may free them afterwards. */
+int psv_plan_create(const psv_grid *grid, const psv_shots *shots, const psv_options *opt,
+                    psv_plan **out);
+int psv_plan_destroy(psv_plan *plan);
+/* Bytes of device memory the plan holds. */
+long long psv_plan_device_bytes(const psv_plan *plan);
+
+/* Sets lam/mu/rho [nz][nx] (host FP64) and derives the staggered averages
+ * and scaled coefficients on the device (mat_av2, n_kernel_lib_PSV.hpp:170). */
+int psv_plan_set_model(psv_plan *plan, const double *lam, const double *mu, const double *rho);
+int psv_plan_get_model(psv_plan *plan, double *lam, double *mu, double *rho);
+/* Observed traces rtf_*_true [nshot][nrec][nt] (read_seismo, h_io_PSV.hpp:34). */
+int psv_plan_set_observed(psv_plan *plan, const double *rtf_uz_true, const double *rtf_ux_true);
+
+/* Forward modelling of every shot (simulate_fwd_PSV's shot loop,
+ * n_simulate_PSV.hpp:23): receiver displacements [nshot][nrec][nt]. */
+int psv_forward(psv_plan *plan, double *rtf_uz, double *rtf_ux);
+
+/* One FWI gradient over every shot, in the reference's order
+ * (simulate_fwi_PSV's shot loop, src/cpu/n_simulate_PSV.cpp:270-419):
+ * forward with snapshots, residual and L2 (adjsrc2), time-reversed adjoint
+ * with the imaging condition, energy weights, interpolation and scaling
+ * added into the plan's global gradients.  The global gradients are NOT
+ * reset (the reference never resets them, :260); see psv_reset_gradient.
+ * L2 = sum over shots.  grad_* (host [nz][nx], may be NULL) receive the
+ * global gradients after the call. */
+int psv_gradient(psv_plan *plan, double *L2, double *grad_lam, double *grad_mu,
+                 double *grad_rho);
+int psv_reset_gradient(psv_plan *plan);
+int psv_get_gradient(psv_plan *plan, double *grad_lam, double *grad_mu, double *grad_rho);
+int psv_set_gradient(psv_plan *plan, const double *grad_lam, const double *grad_mu,
+                     const double *grad_rho);
+
+/* Per-shot outputs of the last psv_gradient for shot ishot: snapped shot
+ * gradients [snap_nz][snap_nx] (kernel_PSV's grad_*), forward / adjoint
+ * energies We, We_adj [nz][nx] (before energy_weights2), modelled traces
+ * [nrec][nt] and the shot's L2.  Any pointer may be NULL. */
+int psv_get_shot_gradient(psv_plan *plan, int ishot, double *grad_lam_shot,
+                          double *grad_mu_shot, double *grad_rho_shot, double *We,
+                          double *We_adj, double *rtf_uz, double *rtf_ux, double *L2);
+
+/* One FWI iteration (src/cpu/n_simulate_PSV.cpp:249-576): copy_mat, the
+ * gradient above, taper2, step_length_PSV with trial forwards of every
+ * shot, and update_mat2 of lam, mu, rho.  *step is the step-length estimate
+ * carried between iterations (in: estimate, out: accepted step).  Outputs:
+ * the iteration's L2, the number of trial forward passes and their (alpha,
+ * L2) pairs in trial_log[2*k] (room for max_trials entries; may be NULL). */
+int psv_fwi_iteration(psv_plan *plan, double *step, double *L2, int *ntrials,
+                      double *trial_log, int max_trials);
+
+/* Trial evaluation used by the step-length search: L2 misfit of the model
+ * updated with step length `step`.  Returns a psv_status. */
+typedef int (*psv_trial_fn)(double step, double *L2, void *ctx);
+
+/* Control flow of step_length_PSV (src/cpu/n_step_length_PSV.cpp:53-209):
+ * halve the estimate until a trial lowers L2 below L2_0, then grow it by
+ * 1.5 until a trial misfit rises again (at most 4 growths), then take the
+ * parabola vertex (psv_calc_opt_step).  *est is the starting estimate in and
+ * the accepted step out.  Trials are logged as (step, L2) pairs in tlog.
+ * Returns PSV_ERR_STEP_SEARCH after 31 halvings without a decrease. */
+int psv_step_length(double *est, double L2_0, psv_trial_fn trial, void *ctx, int *ntrials,
+                    double *tlog, int max_trials);
+
+/* calc_opt_step (include/cpu/n_step_length_PSV.hpp:58): vertex of the
+ * parabola through (sl[i], L2[i]) with the reference's clamps, solved with a
+ * correct 3x3 elimination (the reference's solvelin back-substitution reads
+ * past its arrays, include/cpu/n_solvelin.hpp:37-42). */
+double psv_calc_opt_step(const double *L2, const double *sl);
+
+/* Event-timed device milliseconds of the last forward / gradient /
+ * iteration call, split: [0] forward, [1] adjoint (incl. recompute), [2]
+ * everything else. */
+int psv_last_timing(const psv_plan *plan, double *ms3);
+
+/* The CUDA stream every call of this plan runs on (a cudaStream_t), for
+ * callers that time or order work against it. */
+void *psv_plan_stream(const psv_plan *plan);
+/* Number of kernels this plan has launched so far (graph replays count
+ * their kernel nodes). */
+long long psv_plan_kernel_launches(const psv_plan *plan);
+/* Event-timed profile of the time-step kernels: nsteps forward steps then
+ * nsteps adjoint steps of the first batch, each kernel bracketed by CUDA
+ * events on the plan's stream.  ms6 = mean milliseconds per launch of
+ * {stress, velocity, source/receiver} forward, then the same adjoint.
+ * Needs a model and observed traces; leaves the wavefields undefined. */
+int psv_profile_kernels(psv_plan *plan, int nsteps, double *ms6);
+
+/* ------------------------------------------------------------------------ */
+/* Reference-shaped drop-ins                                                  */
+/* ------------------------------------------------------------------------ */
+
+/* kernel_PSV / kernel_PSV_GPU (include/cpu/n_kernel_PSV.hpp:8-43,
+ * include/cuda/d_kernel_PSV.cuh:9-44): the same arguments in the same
+ * order, with flat host arrays.  One shot, nt steps, forward (grad = 0) or
+ * time-reversed adjoint (grad = 1).  On return the host arrays hold what the
+ * reference leaves in them: final wavefields, energies, the CPML memories
+ * (when non-NULL), receiver traces (forward), the snapshot history (accu),
+ * the snapped shot gradients (grad).  dz_z..dx_x are the reference's
+ * internal derivative scratch arrays: accepted and ignored (may be NULL).
+ * stencil selects PSV_STENCIL_*; precision 32 or 64. */
+int psv_kernel_PSV(int ishot, int nt, int nz, int nx, double dt, double dx, double dz,
+                   int surf, const int *isurf, const double *hc, int fdorder,
+                   double *vz, double *vx, double *uz, double *ux,
+                   double *szz, double *szx, double *sxx, double *We,
+                   double *dz_z, double *dx_z, double *dz_x, double *dx_x,
+                   const double *lam, const double *mu, const double *mu_zx,
+                   const double *rho_zp, const double *rho_xp,
+                   int grad, double *grad_lam, double *grad_mu, double *grad_rho,
+                   int pml_z, const double *a_z, const double *b_z, const double *K_z,
+                   const double *a_half_z, const double *b_half_z, const double *K_half_z,
+                   int pml_x, const double *a_x, const double *b_x, const double *K_x,
+                   const double *a_half_x, const double *b_half_x, const double *K_half_x,
+                   double *mem_vz_z, double *mem_vx_z, double *mem_szz_z, double *mem_szx_z,
+                   double *mem_vz_x, double *mem_vx_x, double *mem_szx_x, double *mem_sxx_x,
+                   int nsrc, int stf_type, const double *stf_z, const double *stf_x,
+                   const int *z_src, const int *x_src, const int *src_shot_to_fire,
+                   int nrec, int rtf_type, double *rtf_uz, double *rtf_ux,
+                   const int *z_rec, const int *x_rec,
+                   int accu, double *accu_vz, double *accu_vx,
+                   double *accu_szz, double *accu_szx, double *accu_sxx,
+                   int snap_z1, int snap_z2, int snap_x1, int snap_x2,
+                   int snap_dt, int snap_dz, int snap_dx, int stencil, int precision);
+
+/* simulate_PSV (include/h_simulate_PSV.hpp:23) run on the GPU: reads
+ * workdir/bin/metaint.bin, intarray.bin, metafloat.bin, mat.bin (and
+ * workdir/io/shot{i}_rtf_u{z,x}.bin for FWI), builds the CPML profiles,
+ * Holberg coefficients and Ricker wavelets as the reference does
+ * (src/h_simulate_PSV.cpp:99-185), then runs forward modelling (writing
+ * bin/shot{i}_rtf_u{z,x}.bin and, with accu_save, bin/shot{i}_{vz,vx,szz,szx,sxx}.bin)
+ * or FWI (writing bin/iter{n}_mat.bin every mat_save_interval iterations).
+ * max_iter caps the FWI iterations (the reference's cap is 1000 with an
+ * early stop after 25, src/cpu/n_simulate_PSV.cpp:240,576-581; 0 = that). */
+int psv_simulate_PSV(const char *workdir, int max_iter, const psv_options *opt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,52 @@
+"""FWI iterations (gradient, taper, step-length search with trial forwards,
+clamped update) on the GPU against the reference's golden run and the
+oracle.  Accepted steps and misfits must follow the same branch sequence
+(identical trial counts)."""
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import engine
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fwi_fp64_matches_reference_golden(gpu):
+    z = np.load(helpers.GOLDEN)
+    name = "fwi_crosswell"
+    sv = helpers.load_case(z, name)
+    with engine.Plan(sv, precision=64) as p:
+        p.set_model(*z[f"{name}/init"])
+        p.set_observed(z[f"{name}/obs_uz"], z[f"{name}/obs_ux"])
+        step = 0.01
+        for it in range(3):
+            r = p.fwi_iteration(step)
+            step = r["step"]
+            assert r["L2"] == pytest.approx(z[f"{name}/L2"][it], rel=1e-9)
+            assert step == pytest.approx(z[f"{name}/step"][it], rel=1e-7)
+        lam, mu, rho = p.get_model()
+        g = p.get_gradient()
+    assert helpers.rel_l2(lam, z[f"{name}/lam"]) < 1e-9
+    assert helpers.rel_l2(mu, z[f"{name}/mu"]) < 1e-9
+    assert helpers.rel_l2(rho, z[f"{name}/rho"]) < 1e-9
+    assert helpers.rel_l2(g[0], z[f"{name}/grad_lam"]) < 1e-8
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_fwi_iterations_match_oracle(gpu, orc, precision):
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, imaging_sign=1)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    niter = 4
+    r = orc.simulate_fwi(sv, *init, uz, ux, niter=niter)
+    assert r["rc"] == 0
+    with engine.Plan(sv, precision=precision) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        step = 0.01
+        for it in range(niter):
+            o = p.fwi_iteration(step)
+            step = o["step"]
+            assert o["ntrials"] == r["trials"][it]
+            rtol = 1e-9 if precision == 64 else 1e-4
+            assert o["L2"] == pytest.approx(r["L2"][it], rel=rtol)
+            assert step == pytest.approx(r["step"][it], rel=1e-6 if precision == 64 else 2e-3)

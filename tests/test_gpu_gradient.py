@@ -1,0 +1,93 @@
+"""FWI gradient on the GPU (forward with snapshots, residual, time-reversed
+adjoint with the imaging condition, energy-weight preconditioning) against
+the FP64 oracle.  Tolerances: FP64 engine 1e-9 relative L2; FP32 engine 1e-4
+relative L2 on the gradients (the stated target)."""
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import engine
+
+pytestmark = pytest.mark.gpu
+RTOL64 = 1e-9
+RTOL32_GRAD = 1e-4
+
+
+def _setup(orc, **kw):
+    sv, true, init = helpers.case(**kw)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    return sv, true, init, uz, ux
+
+
+@pytest.mark.parametrize("kw", [dict(fdorder=4, stencil="holberg", nshot=2, nt=300),
+                                dict(fdorder=2, stencil="reference", nshot=1, nt=300),
+                                dict(fdorder=8, stencil="holberg", nshot=1, nt=250,
+                                     imaging_sign=1)])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_shot_and_global_gradient(gpu, orc, kw, precision):
+    sv, true, init, uz, ux = _setup(orc, **kw)
+    L2_ref, g_ref, shots = helpers.oracle_gradient(orc, sv, init, uz, ux)
+    if sv.imaging_sign > 0:
+        g_ref = [-g for g in g_ref]
+        for o in shots:
+            for k in ("grad_lam", "grad_mu", "grad_rho"):
+                o[k] = -o[k]
+    tol = RTOL64 if precision == 64 else RTOL32_GRAD
+    with engine.Plan(sv, precision=precision) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L2, g = p.gradient()
+        assert L2 == pytest.approx(L2_ref, rel=1e-9 if precision == 64 else 1e-4)
+        for a, b in zip(g, g_ref):
+            assert helpers.rel_l2(a, b) < tol
+        for s in range(sv.nshot):
+            o = p.shot_gradient(s)
+            for k in ("grad_lam", "grad_mu", "grad_rho"):
+                assert helpers.rel_l2(o[k], shots[s][k]) < tol, k
+            for k in ("We", "We_adj"):
+                assert helpers.rel_l2(o[k], shots[s][k]) < (1e-9 if precision == 64 else 1e-4), k
+
+
+def test_gradient_accumulates_across_calls_like_reference(gpu, orc):
+    # the reference never resets the global gradient (n_simulate_PSV.cpp:260)
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nt=200)
+    with engine.Plan(sv, precision=64) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        _, g1 = p.gradient()
+        _, g2 = p.gradient()
+        for a, b in zip(g1, g2):
+            assert helpers.rel_l2(b, 2 * a) < 1e-12
+        p.reset_gradient()
+        _, g3 = p.gradient()
+        for a, b in zip(g1, g3):
+            assert np.array_equal(a, b)
+
+
+def test_subsampled_snapshots_and_interpolation(gpu, orc):
+    # snap_dt, snap_dz, snap_dx > 1, window not divisible by the steps
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nt=240)
+    sv.snap_dt, sv.snap_dz, sv.snap_dx = 3, 2, 3
+    sv.snap_z1, sv.snap_z2, sv.snap_x1, sv.snap_x2 = 5, sv.nz - 9, 7, sv.nx - 10
+    uz, ux = orc.simulate_fwd(sv, *true)
+    L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz, ux)
+    with engine.Plan(sv, precision=64) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L2, g = p.gradient()
+    for a, b in zip(g, g_ref):
+        assert helpers.rel_l2(a, b) < RTOL64
+
+
+def test_batched_gradient_equals_one_shot_at_a_time(gpu, orc):
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=3, nt=200)
+    res = []
+    for mb in (0, 1, 2):
+        with engine.Plan(sv, precision=32, max_batch=mb) as p:
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            res.append(p.gradient())
+    for L2, g in res[1:]:
+        assert L2 == res[0][0]
+        for a, b in zip(g, res[0][1]):
+            assert np.array_equal(a, b)

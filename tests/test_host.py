@@ -1,0 +1,121 @@
+"""Host side of the engine library, no GPU needed: exported symbols, the
+FP64 preprocessing (bitwise against the oracle), the step-length control
+flow, and argument validation."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import _lib, engine
+from fwi_cuda_gb300 import survey as S
+from fwi_cuda_gb300._lib import dptr
+
+
+def header_symbols():
+    text = open(helpers.__file__.replace("tests/helpers.py", "include/fwi_psv.h")).read()
+    return sorted(set(re.findall(r"^[\w\s\*]*?\b(psv_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.lib()
+    names = header_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def test_holberg_cpml_wavelet_bitwise(orc):
+    for fd in (2, 4, 6, 8):
+        assert np.array_equal(S.holbergcoeff(fd), orc.holbergcoeff(fd))
+    for args in [(2.0, 3000.0, 0.001, 1.0, 100.0, 20, 20, 2, 301, 5e-5, 0.5),
+                 (2.0, 800.0, 0.001, 1.0, 200.0, 20, 0, 1, 601, 4e-5, 0.1),
+                 (3.0, 4500.0, 0.0001, 2.0, 60.0, 0, 40, 4, 401, 1e-4, 1.0)]:
+        for a, b in zip(S.cpml_profiles(*args), orc.cpml(*args)):
+            assert np.array_equal(a, b)
+    assert np.array_equal(S.ricker(4000, 5e-5, 100.0), orc.wavelet(4000, 5e-5, 1.0, 100.0))
+
+
+def test_checkfd_matches_oracle(orc):
+    sv, true, _ = helpers.case()
+    lam, mu, rho = true
+    out = np.zeros(4)
+    rc = _lib.lib().psv_checkfd_ssg_elastic(sv.nz, sv.nx, sv.dz, sv.dt, sv.freq_pml,
+                                            sv.npml[1], dptr(rho), dptr(lam), dptr(mu),
+                                            dptr(sv.hc), dptr(out))
+    rc2, out2 = orc.checkfd(sv, lam, mu, rho)
+    assert rc == 0 and rc2 == 0
+    assert np.array_equal(out, out2)
+    # a time step above the limit is reported
+    rc = _lib.lib().psv_checkfd_ssg_elastic(sv.nz, sv.nx, sv.dz, out[0] * 1.01, sv.freq_pml,
+                                            sv.npml[1], dptr(rho), dptr(lam), dptr(mu),
+                                            dptr(sv.hc), dptr(out))
+    assert rc == _lib.PSV_ERR_CFL
+
+
+def _step_length(est, L2_0, f):
+    cb = _lib.TRIAL_FN(lambda a, L, _: (L.__setitem__(0, f(a)), 0)[1])
+    e = C.c_double(est)
+    n = C.c_int()
+    log = np.zeros((64, 2))
+    rc = _lib.lib().psv_step_length(C.byref(e), L2_0, C.cast(cb, C.c_void_p), None, C.byref(n),
+                                    dptr(log), 64)
+    return rc, e.value, n.value, log[:min(n.value, 64)]
+
+
+@pytest.mark.parametrize("fun,est,L0", [
+    (lambda a: (a - 0.037) ** 2, 0.01, 0.037 ** 2),          # grows, brackets, parabola
+    (lambda a: (a - 0.001) ** 2 + 1e-9, 0.01, 1e-6 + 1e-9),  # halves first
+    (lambda a: -a, 0.01, 0.0),                                # never brackets (4 growths)
+    (lambda a: 1.0 + a, 0.01, 0.0),                           # fails after 31 halvings
+])
+def test_step_length_control_flow_matches_oracle(orc, fun, est, L0):
+    rc, step, n, log = _step_length(est, L0, fun)
+    rc2, step2, n2, log2 = orc.step_length(est, L0, fun)
+    assert (rc == 0) == (rc2 == 0)
+    assert n == n2 and np.array_equal(log, log2)
+    if rc == 0:
+        assert step == step2
+    else:
+        assert rc == _lib.PSV_ERR_STEP_SEARCH
+
+
+def test_calc_opt_step_matches_oracle(orc):
+    rng = np.random.default_rng(0)
+    for _ in range(50):
+        sl = np.sort(rng.uniform(0, 0.1, 3))
+        sl[0] = 0.0
+        L2 = rng.uniform(1, 2, 3)
+        assert _lib.lib().psv_calc_opt_step(dptr(L2), dptr(sl)) == orc.calc_opt_step(L2, sl)
+
+
+def _create(sv, **kw):
+    keep = []
+    g, s = sv.grid_struct(keep), sv.shots_struct(keep)
+    o = engine.options(**kw)
+    h = C.c_void_p()
+    rc = _lib.lib().psv_plan_create(C.byref(g), C.byref(s), C.byref(o), C.byref(h))
+    if rc == 0:
+        _lib.lib().psv_plan_destroy(h)
+    return rc
+
+
+def test_plan_validation_errors():
+    sv, _, _ = helpers.case()
+    bad = helpers.case()[0]
+    bad.fdorder = 10
+    assert _create(bad) == _lib.PSV_ERR_UNSUPPORTED
+    bad = helpers.case()[0]
+    bad.x_src = np.array([bad.nx + 3], np.int32)
+    assert _create(bad) == _lib.PSV_ERR_ARG
+    bad = helpers.case()[0]
+    bad.isurf = (bad.isurf[0], 0, 5, 0)  # horizontal + vertical surface
+    assert _create(bad) == _lib.PSV_ERR_UNSUPPORTED
+    bad = helpers.case()[0]
+    bad.snap_z2 = bad.nz + 4
+    assert _create(bad) == _lib.PSV_ERR_ARG
+    assert _create(sv, precision=16) == _lib.PSV_ERR_ARG
+    if not _lib.device_available():
+        assert _create(sv) == _lib.PSV_ERR_CUDA  # valid survey, no device: no CPU fallback
