@@ -178,6 +178,20 @@ def peaks():
 
 
 # ----------------------------------------------------------------------------- our arm
+def run_profile(args):
+    """One FWI gradient of a reduced case for ncu captures (--profile):
+    nt / shots from --nt / --nshot; prints nothing measured."""
+    from fwi_cuda_gb300 import engine
+    sv, true, init = workload(nt=args.nt, nshot=args.nshot)
+    with engine.Plan(sv, precision=32) as p:
+        p.set_model(*true)
+        obs = p.forward()
+        p.set_model(*init)
+        p.set_observed(*obs)
+        L2, _ = p.gradient(fetch=False)
+    print(json.dumps({"profile_case": {"nt": sv.nt, "nshot": sv.nshot, "L2": L2}}))
+
+
 def run_ours(args, rank, world):
     import torch
     from fwi_cuda_gb300 import _lib, engine
@@ -328,7 +342,13 @@ def main():
     ap.add_argument("--ref-nt", type=int, default=400)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fwi", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="one gradient of a reduced case (ncu)")
+    ap.add_argument("--nt", type=int, default=400, help="time steps of the --profile case")
+    ap.add_argument("--nshot", type=int, default=2, help="shots of the --profile case")
     args = ap.parse_args()
+    if args.profile:
+        run_profile(args)
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":

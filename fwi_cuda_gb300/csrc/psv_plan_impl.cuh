@@ -37,8 +37,14 @@ public:
     DevMem fld, memz, memx, hist, gshot, coef, prof, fsb;
     DevMem model, stf, traces, red, taperb, ctl, scales;
     DevMem f_off, f_pos, f_col, f_snap, a_off, a_pos, a_col, a_snap, rec_pos;
-    StepParams<T> sp{};
-    SrcRecParams<T> qf{}, qa{}, qk{};
+    // Checkpointed storage: state checkpoints every K steps, a recompute
+    // state (5 field planes + CPML strips) and a segment snapshot buffer.
+    bool ckpt = false;
+    int K = 0, nck = 0, nslots = 0;
+    long long ck_state = 0;  // elements of one shot's checkpointed state
+    DevMem ck, fld2, memz2, memx2;
+    StepParams<T> sp{}, sp2{};
+    SrcRecParams<T> qf{}, qa{}, qk{}, qr{};
     cudaGraphExec_t gx[NPASS] = {};
     double C[3] = {0, 0, 0};
     double inj = 1.0;     // dt/(dz dx) * max(1/rho): injection gain of a displacement source
@@ -114,10 +120,34 @@ public:
         const double per_shot = (double)(shot_stride + mz_shot + mx_shot + gshot_shot) * sizeof(T);
         const double per_hist = (double)hist_shot * sizeof(T);
         const double shared = 7.0 * plane * sizeof(T) + 12.0 * nz * nx * 8 + 6.0 * nshot * ntr * 8;
-        B = opt.max_batch > 0 ? std::min(opt.max_batch, nshot) : nshot;
-        while (B > 1 && shared + B * (per_shot + per_hist) > budget) B--;
-        if (shared + B * (per_shot + per_hist) > budget && opt.storage == PSV_STORE_FULL)
-            return fail(PSV_ERR_OOM, "full snapshot history of one shot exceeds the HBM budget");
+        // checkpointed alternative: K minimising nt/K states + K/snap_dt snapshots
+        ck_state = 5 * plane + mz_shot + mx_shot;
+        const double snap5 = (double)NHIST * snap_plane, sdt = g.snap_dt;
+        K = opt.checkpoint_interval > 0 ? std::min(opt.checkpoint_interval, g.nt)
+                                        : (int)std::max(1.0, std::round(std::sqrt(g.nt * (double)ck_state * sdt / snap5)));
+        K = std::min(std::max(K, 1), g.nt);
+        nck = (g.nt + K - 1) / K;
+        nslots = (K + g.snap_dt - 1) / g.snap_dt + 1;
+        const double per_ck = ((double)nck * ck_state + (double)ck_state + (double)nslots * snap5) * sizeof(T);
+        auto fit = [&](double extra) {
+            int b = opt.max_batch > 0 ? std::min(opt.max_batch, nshot) : nshot;
+            while (b > 1 && shared + b * (per_shot + extra) > budget) b--;
+            return shared + b * (per_shot + extra) <= budget ? b : 0;
+        };
+        const int b_full = fit(per_hist), b_ck = fit(per_ck);
+        if (opt.storage == PSV_STORE_FULL) {
+            if (!b_full) return fail(PSV_ERR_OOM, "full snapshot history of one shot exceeds the HBM budget");
+            B = b_full;
+        } else if (opt.storage == PSV_STORE_CHECKPOINT) {
+            if (!b_ck) return fail(PSV_ERR_OOM, "checkpoints of one shot exceed the HBM budget");
+            ckpt = true;
+            B = b_ck;
+        } else {
+            if (!b_full && !b_ck) return fail(PSV_ERR_OOM, "one shot does not fit the HBM budget");
+            ckpt = b_ck > b_full;
+            B = ckpt ? b_ck : b_full;
+        }
+        if (ckpt) hist_shot = (long long)nslots * NHIST * snap_plane;
         nbatch = (nshot + B - 1) / B;
 
         PSV_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -350,6 +380,10 @@ public:
         qa.stf_shot_stride = ntr; qa.stf_ncol = sv.s.nrec; qa.stf_type = sv.s.rtf_type;
         qa.rtf_z = qa.rtf_x = nullptr;
         qa.amp_scale = ascale();
+        qr = qf;  // recomputed forward: sources and snapshot fix-ups, no recording
+        qr.rtf_z = qr.rtf_x = nullptr;
+        sp2 = p;  // recompute state: 5 planes per shot and its own CPML strips
+        sp2.shot_stride = 5 * plane;
     }
 
     int ensure_hist()
@@ -357,7 +391,43 @@ public:
         if (hist.p || hist_shot == 0) return PSV_OK;
         PSV_TRY(hist.alloc((size_t)B * hist_shot * sizeof(T), total));
         sp.hist = hist.as<T>();
+        if (ckpt) {
+            PSV_TRY(ck.alloc((size_t)nck * B * ck_state * sizeof(T), total));
+            PSV_TRY(fld2.alloc((size_t)B * 5 * plane * sizeof(T), total));
+            PSV_TRY(memz2.alloc((size_t)B * mz_shot * sizeof(T), total));
+            PSV_TRY(memx2.alloc((size_t)B * mx_shot * sizeof(T), total));
+            sp2.fld = fld2.as<T>();
+            sp2.memz = memz2.as<T>();
+            sp2.memx = memx2.as<T>();
+        }
+        sp2.hist = hist.as<T>();
         drop_graphs();
+        return PSV_OK;
+    }
+
+    // Copy the forward state of the batch into / out of checkpoint j.
+    int ck_copy(int j, bool save)
+    {
+        T *c = ck.as<T>() + (size_t)j * B * ck_state;
+        const size_t cp = (size_t)ck_state * sizeof(T);
+        T *f = save ? fld.as<T>() : fld2.as<T>();
+        const size_t fp = (size_t)(save ? shot_stride : 5 * plane) * sizeof(T);
+        T *mz = save ? memz.as<T>() : memz2.as<T>();
+        T *mx = save ? memx.as<T>() : memx2.as<T>();
+        const size_t w = (size_t)5 * plane * sizeof(T);
+        if (save) PSV_CU(cudaMemcpy2DAsync(c, cp, f, fp, w, B, cudaMemcpyDeviceToDevice, st));
+        else PSV_CU(cudaMemcpy2DAsync(f, fp, c, cp, w, B, cudaMemcpyDeviceToDevice, st));
+        if (mz_shot) {
+            const size_t zw = (size_t)mz_shot * sizeof(T);
+            if (save) PSV_CU(cudaMemcpy2DAsync(c + 5 * plane, cp, mz, zw, zw, B, cudaMemcpyDeviceToDevice, st));
+            else PSV_CU(cudaMemcpy2DAsync(mz, zw, c + 5 * plane, cp, zw, B, cudaMemcpyDeviceToDevice, st));
+        }
+        if (mx_shot) {
+            const size_t xw = (size_t)mx_shot * sizeof(T);
+            T *cx = c + 5 * plane + mz_shot;
+            if (save) PSV_CU(cudaMemcpy2DAsync(cx, cp, mx, xw, xw, B, cudaMemcpyDeviceToDevice, st));
+            else PSV_CU(cudaMemcpy2DAsync(mx, xw, cx, cp, xw, B, cudaMemcpyDeviceToDevice, st));
+        }
         return PSV_OK;
     }
 
@@ -396,15 +466,49 @@ public:
         }
         PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
-        for (int jt = 0; jt < nt; jt++) {
-            const int it = adj ? nt - 1 - jt : jt;
-            const bool snap = !(it % sdt);
-            PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
-            PSV_CU(launch_velocity<T>(sp, sv.ns, mode, (snap && (store || adj)) ? it / sdt : -1, blk,
-                                      B, st));
-            PSV_CU(launch_srcrec<T>(sp, q, it, (snap && store) ? it / sdt : -1, B, st));
+        long long nk = (mode == MODE_ADJ ? 5 : mode == MODE_FWD ? 4 : 3);
+        if (ckpt && kind == PASS_FWD_STORE) {
+            // forward keeping a state checkpoint at the start of every K-step segment
+            for (int it = 0; it < nt; it++) {
+                if (!(it % K)) PSV_TRY(ck_copy(it / K, true));
+                PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
+                PSV_CU(launch_velocity<T>(sp, sv.ns, mode, -1, blk, B, st));
+                PSV_CU(launch_srcrec<T>(sp, qf, it, -1, B, st));
+            }
+            nk += 3LL * nt;
+        } else if (ckpt && kind == PASS_ADJ_RES) {
+            // segments in reverse: recompute the forward from the checkpoint into
+            // the segment snapshot buffer, then the segment's adjoint steps
+            for (int j = nck - 1; j >= 0; j--) {
+                const int a = j * K, e = std::min(a + K, nt);
+                const int base = (a + sdt - 1) / sdt;
+                PSV_TRY(ck_copy(j, false));
+                for (int it = a; it < e; it++) {
+                    const int slot = !(it % sdt) ? it / sdt - base : -1;
+                    PSV_CU(launch_stress<T>(sp2, sv.ns, blk, B, st));
+                    PSV_CU(launch_velocity<T>(sp2, sv.ns, MODE_FWD_NOWE, slot, blk, B, st));
+                    PSV_CU(launch_srcrec<T>(sp2, qr, it, slot, B, st));
+                }
+                for (int it = e - 1; it >= a; it--) {
+                    const int slot = !(it % sdt) ? it / sdt - base : -1;
+                    PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
+                    PSV_CU(launch_velocity<T>(sp, sv.ns, MODE_ADJ, slot, blk, B, st));
+                    PSV_CU(launch_srcrec<T>(sp, qa, it, -1, B, st));
+                }
+            }
+            nk += 6LL * nt;
+        } else {
+            for (int jt = 0; jt < nt; jt++) {
+                const int it = adj ? nt - 1 - jt : jt;
+                const bool snap = !(it % sdt);
+                PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
+                PSV_CU(launch_velocity<T>(sp, sv.ns, mode, (snap && (store || adj)) ? it / sdt : -1,
+                                          blk, B, st));
+                PSV_CU(launch_srcrec<T>(sp, q, it, (snap && store) ? it / sdt : -1, B, st));
+            }
+            nk += 3LL * nt;
         }
-        nlaunch = n0 + 3LL * nt + (mode == MODE_ADJ ? 5 : mode == MODE_FWD ? 4 : 3);
+        nlaunch = n0 + nk;
         return PSV_OK;
     }
 
@@ -797,7 +901,7 @@ public:
             const SrcRecParams<T> &q = adj ? qa : qf;
             for (int j = 0; j < nsteps; j++) {
                 const int it = adj ? nt - 1 - j : j;
-                const int slot = !(it % sdt) ? it / sdt : -1;
+                const int slot = !(it % sdt) ? (it / sdt) % (ckpt ? nslots : sv.snt) : -1;
                 cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
                 cudaEventRecord(E[0], st);
                 cudaError_t c = launch_stress<T>(sp, sv.ns, blk, B, st);

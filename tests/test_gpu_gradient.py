@@ -26,12 +26,7 @@ def _setup(orc, **kw):
 @pytest.mark.parametrize("precision", [64, 32])
 def test_shot_and_global_gradient(gpu, orc, kw, precision):
     sv, true, init, uz, ux = _setup(orc, **kw)
-    L2_ref, g_ref, shots = helpers.oracle_gradient(orc, sv, init, uz, ux)
-    if sv.imaging_sign > 0:
-        g_ref = [-g for g in g_ref]
-        for o in shots:
-            for k in ("grad_lam", "grad_mu", "grad_rho"):
-                o[k] = -o[k]
+    L2_ref, g_ref, shots = helpers.oracle_gradient(orc, sv, init, uz, ux)  # oracle honours imaging_sign
     tol = RTOL64 if precision == 64 else RTOL32_GRAD
     with engine.Plan(sv, precision=precision) as p:
         p.set_model(*init)
@@ -91,3 +86,37 @@ def test_batched_gradient_equals_one_shot_at_a_time(gpu, orc):
         assert L2 == res[0][0]
         for a, b in zip(g, res[0][1]):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision,interval", [(32, 0), (32, 7), (64, 50)])
+def test_checkpointed_gradient_bitwise_equals_full_storage(gpu, orc, precision, interval):
+    # recomputation from checkpoints is deterministic: stated bound = 0
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=2, nt=301,
+                                    snap_dt=2)
+    res = {}
+    for storage in ("full", "checkpoint"):
+        with engine.Plan(sv, precision=precision, storage=storage,
+                         checkpoint_interval=interval) as p:
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            res[storage] = (p.gradient(), [p.shot_gradient(s) for s in range(sv.nshot)])
+    (L2a, ga), sa = res["full"]
+    (L2b, gb), sb = res["checkpoint"]
+    assert L2a == L2b
+    for a, b in zip(ga, gb):
+        assert np.array_equal(a, b)
+    for x, y in zip(sa, sb):
+        for k in ("grad_lam", "grad_mu", "grad_rho", "We", "We_adj"):
+            assert np.array_equal(x[k], y[k]), k
+
+
+def test_checkpoint_storage_uses_less_memory(gpu, orc):
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=2, nt=600)
+    mem = {}
+    for storage in ("full", "checkpoint"):
+        with engine.Plan(sv, storage=storage) as p:
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            p.gradient(fetch=False)
+            mem[storage] = p.device_bytes
+    assert mem["checkpoint"] < 0.5 * mem["full"]
