@@ -269,6 +269,35 @@ int psv_fwi_iteration(psv_plan *p, double *step, double *L2, int *ntrials, doubl
     return p->impl->fwi_iteration(step, L2, ntrials, tlog, maxt);
 }
 
+int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
+               const double *true_x, double *res_z, double *res_x, int nshot, int nrec, int nt,
+               double dt, double *L2)
+{
+    if (!mod_z || !mod_x || !true_z || !true_x || !L2 || nshot <= 0 || nrec < 0 || nt < 0)
+        return fail(PSV_ERR_ARG, "misfit: null array or bad size");
+    if (!psv_device_available()) return fail(PSV_ERR_CUDA, "no CUDA device available");
+    const long long n = (long long)nrec * nt;
+    const size_t bytes = (size_t)nshot * n * sizeof(double);
+    size_t total = 0;
+    DevMem d[6], part, out;
+    for (auto &m : d) PSV_TRY(m.alloc(bytes + 8, total));
+    PSV_TRY(part.alloc((size_t)256 * nshot * sizeof(double), total));
+    PSV_TRY(out.alloc((size_t)nshot * sizeof(double), total));
+    const double *src[4] = {mod_z, mod_x, true_z, true_x};
+    for (int k = 0; k < 4; k++) PSV_CU(cudaMemcpy(d[k].p, src[k], bytes, cudaMemcpyHostToDevice));
+    const bool want_res = res_z && res_x;
+    PSV_CU(launch_adjsrc(d[0].as<double>(), d[1].as<double>(), d[2].as<double>(),
+                         d[3].as<double>(), want_res ? d[4].as<double>() : nullptr,
+                         want_res ? d[5].as<double>() : nullptr, n, nshot, dt,
+                         part.as<double>(), out.as<double>(), 0));
+    PSV_CU(cudaMemcpy(L2, out.p, nshot * sizeof(double), cudaMemcpyDeviceToHost));
+    if (want_res) {
+        PSV_CU(cudaMemcpy(res_z, d[4].p, bytes, cudaMemcpyDeviceToHost));
+        PSV_CU(cudaMemcpy(res_x, d[5].p, bytes, cudaMemcpyDeviceToHost));
+    }
+    return PSV_OK;
+}
+
 void *psv_plan_stream(const psv_plan *p) { return p && p->impl ? p->impl->stream() : nullptr; }
 
 long long psv_plan_kernel_launches(const psv_plan *p) { return p && p->impl ? p->impl->launches() : 0; }

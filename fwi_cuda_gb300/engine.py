@@ -155,6 +155,20 @@ class Plan:
         return dict(forward_ms=t[0], adjoint_ms=t[1], other_ms=t[2])
 
 
+def misfit(mod_uz, mod_ux, true_uz, true_ux, dt, residual=True):
+    """adjsrc2 for [nshot][nrec][nt] traces on the GPU: (L2 per shot, res_z, res_x)."""
+    m = [f64(a) for a in (mod_uz, mod_ux, true_uz, true_ux)]
+    if m[0].ndim == 2:
+        m = [a[None] for a in m]
+    nshot, nrec, nt = m[0].shape
+    L2 = np.zeros(nshot)
+    rz = np.zeros_like(m[0]) if residual else None
+    rx = np.zeros_like(m[0]) if residual else None
+    check(_lib.lib().psv_misfit(*[dptr(a) for a in m], dptr(rz), dptr(rx), nshot, nrec, nt, dt,
+                                dptr(L2)))
+    return L2, rz, rx
+
+
 def kernel_PSV(ishot, nt, nz, nx, dt, dx, dz, surf, isurf, hc, fdorder, lam, mu, mu_zx, rho_zp,
                rho_xp, grad, pml_z, cpml_z, pml_x, cpml_x, nsrc, stf_type, stf_z, stf_x, z_src,
                x_src, src_shot_to_fire, nrec, rtf_type, z_rec, x_rec, accu, snap, history=None,

@@ -181,6 +181,15 @@ int psv_get_shot_gradient(psv_plan *plan, int ishot, double *grad_lam_shot,
 int psv_fwi_iteration(psv_plan *plan, double *step, double *L2, int *ntrials,
                       double *trial_log, int max_trials);
 
+/* adjsrc2 (include/cpu/n_kernel_lib_PSV.hpp:139) for nshot shots at once on
+ * the GPU: residuals res = mod - true and L2[s] = sum over the shot's traces
+ * of dt/2 (r_z^2 + r_x^2).  Host arrays [nshot][nrec][nt]; res_* may alias
+ * mod_* (the reference overwrites its model traces, n_simulate_PSV.cpp:320)
+ * or be NULL.  The sum runs in a fixed order (deterministic). */
+int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
+               const double *true_x, double *res_z, double *res_x, int nshot, int nrec, int nt,
+               double dt, double *L2);
+
 /* Trial evaluation used by the step-length search: L2 misfit of the model
  * updated with step length `step`.  Returns a psv_status. */
 typedef int (*psv_trial_fn)(double step, double *L2, void *ctx);

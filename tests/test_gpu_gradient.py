@@ -120,3 +120,15 @@ def test_checkpoint_storage_uses_less_memory(gpu, orc):
             p.gradient(fetch=False)
             mem[storage] = p.device_bytes
     assert mem["checkpoint"] < 0.5 * mem["full"]
+
+
+def test_misfit_entry_point_matches_oracle(gpu, orc):
+    rng = np.random.default_rng(5)
+    mod = rng.standard_normal((3, 17, 301)) * 1e-9
+    obs = mod + rng.standard_normal(mod.shape) * 1e-11
+    modx, obsx = mod[:, ::-1].copy(), obs[:, ::-1].copy()
+    L2, rz, rx = engine.misfit(mod, modx, obs, obsx, 5e-5)
+    for s in range(3):
+        L2o, az, ax = orc.adjsrc2(mod[s], modx[s], obs[s], obsx[s], 5e-5)
+        assert L2[s] == pytest.approx(L2o, rel=1e-13)
+        assert np.array_equal(rz[s], az) and np.array_equal(rx[s], ax)
