@@ -90,6 +90,8 @@ SIGNATURES = {
     "psv_fwi_iteration": (C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp, C.c_int]),
     "psv_last_timing": (C.c_int, [C.c_void_p, _dp]),
     "psv_misfit": (C.c_int, [_dp] * 6 + [C.c_int, C.c_int, C.c_int, C.c_double, _dp]),
+    "psv_misfit_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_int, C.c_int, C.c_int, C.c_double,
+                                                          C.c_void_p, C.c_void_p]),
     "psv_plan_stream": (C.c_void_p, [C.c_void_p]),
     "psv_plan_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "psv_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, _dp]),

@@ -34,6 +34,7 @@ UNITS = [
     ("psv_plan_f32.cu", []),
     ("psv_plan_f64.cu", []),
     ("psv_capi.cu", []),
+    ("psv_noalloc.cu", []),
     ("psv_host.cpp", []),
 ]
 

@@ -190,6 +190,28 @@ int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
                const double *true_x, double *res_z, double *res_x, int nshot, int nrec, int nt,
                double dt, double *L2);
 
+/* psv_misfit for callers that cannot allocate device memory.  No counterpart
+ * in the reference.  Some callers may not call cudaMalloc: code whose GPU
+ * memory is owned by a framework allocator or a fixed pool, a caller that is
+ * recording a CUDA graph (allocation is not allowed during stream capture),
+ * or a latency-bound loop that must avoid allocation.  They pass DEVICE
+ * pointers for every input and output (traces [nshot][nrec][nt], residuals
+ * optional as a pair, d_L2[nshot]); the only scratch, the reduction's partial
+ * sums, lives in a fixed device array inside the library (2 MiB, held by each
+ * GPU that loads the library until exit), so nshot is limited to
+ * PSV_MISFIT_NOALLOC_MAX_SHOTS (larger values return PSV_ERR_ARG).  Work is
+ * enqueued on `stream` (a cudaStream_t, NULL = default stream) and not
+ * synchronised.  The first call on a device looks up the array's device
+ * address (once per device, with that device current): make that first call
+ * before any stream capture.  All calls share the array, so calls that
+ * overlap on the GPU (different streams, or several devices' threads
+ * enqueueing concurrently on one device) race; order them on one stream.
+ * Results equal psv_misfit's. */
+#define PSV_MISFIT_NOALLOC_MAX_SHOTS 1024
+int psv_misfit_noalloc(const double *d_mod_z, const double *d_mod_x, const double *d_true_z,
+                       const double *d_true_x, double *d_res_z, double *d_res_x, int nshot,
+                       int nrec, int nt, double dt, double *d_L2, void *stream);
+
 /* Trial evaluation used by the step-length search: L2 misfit of the model
  * updated with step length `step`.  Returns a psv_status. */
 typedef int (*psv_trial_fn)(double step, double *L2, void *ctx);
