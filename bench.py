@@ -281,7 +281,7 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return None
-    shares = {k: v for k, v in prof.items() if not k.startswith("srcrec")}
+    shares = dict(prof)
     top = max(shares, key=shares.get)
     pts = CFG["nz"] * CFG["nx"] * nshot
     alg = algorithmic_bytes(top, CFG["snap_dt"]) * pts

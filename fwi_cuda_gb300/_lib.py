@@ -59,7 +59,8 @@ class PsvOptions(C.Structure):
     _fields_ = [
         ("precision", C.c_int), ("storage", C.c_int), ("hbm_budget_gb", C.c_double),
         ("checkpoint_interval", C.c_int), ("max_batch", C.c_int), ("use_graphs", C.c_int),
-        ("block_x", C.c_int), ("block_y", C.c_int),
+        ("block_x", C.c_int), ("block_y", C.c_int), ("rows_per_thread", C.c_int),
+        ("autotune", C.c_int),
     ]
 
 
@@ -89,12 +90,17 @@ SIGNATURES = {
     "psv_get_shot_gradient": (C.c_int, [C.c_void_p, C.c_int] + [_dp] * 8),
     "psv_fwi_iteration": (C.c_int, [C.c_void_p, _dp, _dp, _ip, _dp, C.c_int]),
     "psv_last_timing": (C.c_int, [C.c_void_p, _dp]),
+    "psv_save_model": (C.c_int, [C.c_void_p]),
+    "psv_taper_gradient": (C.c_int, [C.c_void_p]),
+    "psv_trial_misfit": (C.c_int, [C.c_void_p, C.c_double, _dp]),
+    "psv_update_model": (C.c_int, [C.c_void_p, C.c_double]),
     "psv_misfit": (C.c_int, [_dp] * 6 + [C.c_int, C.c_int, C.c_int, C.c_double, _dp]),
     "psv_misfit_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_int, C.c_int, C.c_int, C.c_double,
                                                           C.c_void_p, C.c_void_p]),
     "psv_plan_stream": (C.c_void_p, [C.c_void_p]),
     "psv_plan_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "psv_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, _dp]),
+    "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
     "psv_step_length": (C.c_int, [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp, C.c_int]),
     "psv_calc_opt_step": (C.c_double, [_dp, _dp]),
     "psv_kernel_PSV": (C.c_int,
@@ -108,7 +114,7 @@ SIGNATURES = {
                        + [C.c_int, C.c_int, _dp, _dp, _ip, _ip]
                        + [C.c_int] + [_dp] * 5
                        + [C.c_int] * 7 + [C.c_int, C.c_int]),
-    "psv_simulate_PSV": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(PsvOptions)]),
+    "psv_simulate_PSV": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.POINTER(PsvOptions)]),
 }
 
 TRIAL_FN = C.CFUNCTYPE(C.c_int, C.c_double, _dp, C.c_void_p)

@@ -172,6 +172,7 @@ void psv_options_default(psv_options *o)
     o->storage = PSV_STORE_AUTO;
     o->hbm_budget_gb = 180.0;
     o->use_graphs = 1;
+    o->autotune = 1;
 }
 
 int psv_plan_create(const psv_grid *g, const psv_shots *s, const psv_options *opt, psv_plan **out)
@@ -302,11 +303,42 @@ void *psv_plan_stream(const psv_plan *p) { return p && p->impl ? p->impl->stream
 
 long long psv_plan_kernel_launches(const psv_plan *p) { return p && p->impl ? p->impl->launches() : 0; }
 
+int psv_plan_autotune(psv_plan *p, int nsteps, int *rpt, int *by)
+{
+    PLAN_CHECK(p);
+    return p->impl->autotune(nsteps, rpt, by);
+}
+
 int psv_profile_kernels(psv_plan *p, int nsteps, double *ms6)
 {
     PLAN_CHECK(p);
     if (!ms6) return fail(PSV_ERR_ARG, "null output");
     return p->impl->profile(nsteps, ms6);
+}
+
+int psv_save_model(psv_plan *p)
+{
+    PLAN_CHECK(p);
+    return p->impl->save_model();
+}
+
+int psv_taper_gradient(psv_plan *p)
+{
+    PLAN_CHECK(p);
+    return p->impl->taper_gradient();
+}
+
+int psv_trial_misfit(psv_plan *p, double step, double *L2)
+{
+    PLAN_CHECK(p);
+    if (!L2) return fail(PSV_ERR_ARG, "null L2 output");
+    return p->impl->trial_misfit(step, L2);
+}
+
+int psv_update_model(psv_plan *p, double step)
+{
+    PLAN_CHECK(p);
+    return p->impl->update_model(step);
 }
 
 int psv_last_timing(const psv_plan *p, double *ms3)
@@ -378,7 +410,7 @@ int psv_kernel_PSV(int ishot, int nt, int nz, int nx, double dt, double dx, doub
 }
 
 // simulate_PSV (src/h_simulate_PSV.cpp:92-258) on the GPU.
-int psv_simulate_PSV(const char *workdir, int max_iter, const psv_options *opt)
+int psv_simulate_PSV(const char *workdir, int max_iter, int imaging_sign, const psv_options *opt)
 {
     if (!workdir) return fail(PSV_ERR_ARG, "null workdir");
     const std::string dir(workdir);
@@ -417,6 +449,7 @@ int psv_simulate_PSV(const char *workdir, int max_iter, const psv_options *opt)
     g.snap_z1 = in.snap_z1; g.snap_z2 = in.snap_z2; g.snap_x1 = in.snap_x1; g.snap_x2 = in.snap_x2;
     g.snap_dt = in.snap_dt; g.snap_dz = in.snap_dz; g.snap_dx = in.snap_dx;
     for (int k = 0; k < 8; k++) g.taper[k] = in.taper[k];
+    g.imaging_sign = imaging_sign;
     psv_shots s{};
     s.nshot = in.nshot; s.nsrc = in.nsrc; s.nrec = in.nrec; s.stf_type = in.stf_type;
     s.rtf_type = in.rtf_type; s.z_src = in.z_src.data(); s.x_src = in.x_src.data();

@@ -1,12 +1,13 @@
 // psv_kernels.cuh -- sm_103a kernels of the P/SV velocity-stress time loop.
 //
 // One time step of the reference loop (src/cpu/n_kernel_PSV.cpp:90-210) is
-// three launches here instead of eight full-grid passes:
+// two launches here instead of eight full-grid passes:
 //   k_stress    vdiff2 + pml_diff2 + update_s2 + surf_mirror   (:107-128)
 //   k_velocity  sdiff2 + pml_diff2 + update_v2, fused with the snapshot
 //               store gard_fwd_storage2 (forward) or the imaging condition
-//               fwi_grad2 (adjoint)                             (:138-150,191-206)
-//   k_srcrec    vsrc2 + urec2, one block per shot               (:164-175)
+//               fwi_grad2 (adjoint)                             (:138-150,191-206),
+//               and vsrc2 + urec2 for the sources and receivers of each
+//               block's tile                                    (:164-175)
 // Derivatives never leave registers, CPML memories exist only on the
 // absorbing strips, and every shot of a batch is one blockIdx.z slice.
 #pragma once
@@ -88,6 +89,23 @@ struct SrcRecParams {
     // rec_unscale[shot] = 1 / amp_scale[shot].  Keeps FP32 wavefields of
     // physical-unit surveys away from the denormal range.
     const double *amp_scale, *rec_unscale;  // [nshot]
+    // Sources and receivers by tile of the velocity kernel (32 columns x tz
+    // rows), so the block that owns a cell injects / records it:
+    //   src_kind 0: the shot's sources, t_src_off[shot][ntiles + 1] into
+    //               t_src_k (entries index src_pos / src_col / src_snap);
+    //   src_kind 1: every receiver fires its column of the stf array;
+    //   src_kind -1: nothing is injected.
+    int src_kind, ntiles;
+    const int *t_src_off, *t_src_k;
+    const int *t_rec_off, *t_rec_r;  // [ntiles + 1] into receiver indices
 };
+
+// Rows per thread of the stencil kernels: 1, 2 or 4 (FP32); negative values
+// select the warp-shuffle variant with |r| rows.  FP64 always uses 1.
+template <typename T> inline int rpt_ok(int r)
+{
+    if (sizeof(T) == 8) return 1;
+    return (r == 1 || r == 2 || r == 4 || r == -2 || r == -4) ? r : 1;
+}
 
 }  // namespace psv

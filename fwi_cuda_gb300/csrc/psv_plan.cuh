@@ -14,12 +14,11 @@
 
 namespace psv {
 
-template <typename T> cudaError_t launch_stress(const StepParams<T> &, int, dim3, int, cudaStream_t);
 template <typename T>
-cudaError_t launch_velocity(const StepParams<T> &, int, int, int, dim3, int, cudaStream_t);
+cudaError_t launch_stress(const StepParams<T> &, int ns, int rpt, dim3, int, cudaStream_t);
 template <typename T>
-cudaError_t launch_srcrec(const StepParams<T> &, const SrcRecParams<T> &, int, int, int,
-                          cudaStream_t);
+cudaError_t launch_velocity(const StepParams<T> &, const SrcRecParams<T> &, int ns, int mode,
+                            int it, int slot, int rpt, dim3, int, cudaStream_t);
 template <typename T>
 cudaError_t launch_zero_planes(T *base, long long shot_stride, long long off, long long count,
                                int nbatch, cudaStream_t st);
@@ -70,6 +69,7 @@ struct DevMem {
     }
     int alloc(size_t n, size_t &total)
     {
+        total -= bytes;
         release();
         if (n == 0) return PSV_OK;
         cudaError_t e = cudaMalloc(&p, n);
@@ -101,10 +101,15 @@ struct PlanIface {
     virtual int get_shot(int ishot, double *gl, double *gm, double *gr, double *We, double *WeA,
                          double *uz, double *ux, double *L2) = 0;
     virtual int fwi_iteration(double *step, double *L2, int *ntrials, double *tlog, int maxt) = 0;
+    virtual int save_model() = 0;
+    virtual int taper_gradient() = 0;
+    virtual int update_model(double step) = 0;
+    virtual int trial_misfit(double step, double *L2) = 0;
     virtual int timing(double *ms3) const = 0;
     virtual void *stream() const = 0;
     virtual long long launches() const = 0;
     virtual int profile(int nsteps, double *ms6) = 0;
+    virtual int autotune(int nsteps, int *rpt, int *by) = 0;
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
                             const double *rho_zp, const double *rho_xp, int ishot, int grad,

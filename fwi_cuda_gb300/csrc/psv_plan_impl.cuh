@@ -4,12 +4,29 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "psv_plan.cuh"
 
 namespace psv {
 
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// Process-wide cache of autotuned tile shapes: (nz, nx, stencil terms, batch,
+// element size, interior rows) -> (rows per thread, block height).
+using TuneKey = std::tuple<int, int, int, int, int, int>;
+inline std::map<TuneKey, std::pair<int, int>> &tune_cache()
+{
+    static std::map<TuneKey, std::pair<int, int>> m;
+    return m;
+}
+inline std::mutex &tune_mutex()
+{
+    static std::mutex m;
+    return m;
+}
 
 // Which time loop a pass runs.
 enum PassKind {
@@ -37,6 +54,9 @@ public:
     DevMem fld, memz, memx, hist, gshot, coef, prof, fsb;
     DevMem model, stf, traces, red, taperb, ctl, scales;
     DevMem f_off, f_pos, f_col, f_snap, a_off, a_pos, a_col, a_snap, rec_pos;
+    DevMem t_src_off, t_src_k, t_rec_off, t_rec_r;  // per-tile source / receiver index
+    int rpt = 1;                                     // rows per thread (< 0: shuffle variant)
+    std::vector<int> h_f_off;                        // host copy of the per-shot source lists
     // Checkpointed storage: state checkpoints every K steps, a recompute
     // state (5 field planes + CPML strips) and a segment snapshot buffer.
     bool ckpt = false;
@@ -53,6 +73,7 @@ public:
     int last_s0 = -1, last_n = 0, last_batch_s0 = 0;
     double t_ms[3] = {0, 0, 0};
     bool have_model = false, have_obs = false, store_flag = false;
+    bool tuned = false;
     long long nlaunch = 0;          // kernels launched (graph nodes counted per replay)
     long long gx_nodes[NPASS] = {}; // kernels in each captured pass
     dim3 blk{32, 8, 1};
@@ -89,6 +110,8 @@ public:
     double *fscale() const { return scales.as<double>(); }
     double *funscale() const { return fscale() + sv.s.nshot; }
     double *ascale() const { return fscale() + 2 * sv.s.nshot; }
+    int ntiles = 0;
+    std::vector<int> src_list_col;  // source index of each entry of the per-shot lists
     unsigned long long *rmax() const { return (unsigned long long *)(fscale() + 3 * sv.s.nshot); }
 
     // ---------------------------------------------------------------- setup
@@ -99,9 +122,9 @@ public:
         const psv_grid &g = sv.g;
         const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
         const int al = 128 / (int)sizeof(T);
-        if (opt.block_x > 0 && opt.block_y > 0 && opt.block_x * opt.block_y <= 256 &&
-            opt.block_x % 32 == 0)
-            blk = dim3(opt.block_x, opt.block_y, 1);
+        if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
+        if (opt.block_y > 0 || opt.rows_per_thread) opt.autotune = 0;  // explicit shape wins
+        rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
         pitch = round_up(nx, al);
         plane = (long long)nz * pitch;
         shot_stride = NFIELD * plane;
@@ -228,8 +251,10 @@ public:
                 }
             off[s + 1] = (int)pos.size();
         }
+        h_f_off = off;
         PSV_TRY(put(f_off, off));
         PSV_TRY(put(f_pos, pos));
+        src_list_col = col;
         PSV_TRY(put(f_col, col));
         PSV_TRY(put(f_snap, snap));
         std::vector<int> aoff(nshot + 1), apos, acol, asnap, rpos(nrec);
@@ -248,6 +273,7 @@ public:
         PSV_TRY(put(a_col, acol));
         PSV_TRY(put(a_snap, asnap));
         PSV_TRY(put(rec_pos, rpos));
+        PSV_TRY(build_tile_index());
         // stf [nsrc][nt] -> [nt][nsrc]
         std::vector<double> h((size_t)2 * nt * std::max(nsrc, 1), 0.0);
         for (int is = 0; is < nsrc; is++)
@@ -258,6 +284,45 @@ public:
         PSV_TRY(stf.alloc(h.size() * 8, total));
         PSV_CU(cudaMemcpyAsync(stf.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, st));
         PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    // Sources and receivers bucketed by the velocity kernel's tiles (32
+    // columns x blk.y * rpt rows), so each block finds its own.
+    int build_tile_index()
+    {
+        const int nshot = sv.s.nshot, nrec = sv.s.nrec;
+        const int tz = (int)blk.y * (rpt < 0 ? -rpt : rpt), ntx = (sv.g.nx + 31) / 32, ntz = (sv.g.nz + tz - 1) / tz;
+        const int nt_ = ntx * ntz;
+        auto tile_of = [&](int z, int x) { return (z / tz) * ntx + x / 32; };
+        std::vector<int> soff((size_t)nshot * (nt_ + 1), 0), sk;
+        std::vector<std::vector<int>> b(nt_);
+        for (int s_ = 0; s_ < nshot; s_++) {
+            for (auto &v : b) v.clear();
+            for (int j = h_f_off[s_]; j < h_f_off[s_ + 1]; j++) {
+                const int is = src_list_col[j];
+                b[tile_of(sv.z_src[is], sv.x_src[is])].push_back(j);
+            }
+            int *o = &soff[(size_t)s_ * (nt_ + 1)];
+            for (int t = 0; t < nt_; t++) {
+                o[t] = (int)sk.size();
+                sk.insert(sk.end(), b[t].begin(), b[t].end());
+            }
+            o[nt_] = (int)sk.size();
+        }
+        std::vector<int> roff(nt_ + 1, 0), rr;
+        for (auto &v : b) v.clear();
+        for (int r = 0; r < nrec; r++) b[tile_of(sv.z_rec[r], sv.x_rec[r])].push_back(r);
+        for (int t = 0; t < nt_; t++) {
+            roff[t] = (int)rr.size();
+            rr.insert(rr.end(), b[t].begin(), b[t].end());
+        }
+        roff[nt_] = (int)rr.size();
+        ntiles = nt_;
+        PSV_TRY(put(t_src_off, soff));
+        PSV_TRY(put(t_src_k, sk));
+        PSV_TRY(put(t_rec_off, roff));
+        PSV_TRY(put(t_rec_r, rr));
         return PSV_OK;
     }
 
@@ -370,6 +435,9 @@ public:
         q.rtf_shot_stride = ntr;
         q.dt_d = g.dt; q.dzdx = g.dz * g.dx; q.nt = g.nt;
         q.amp_scale = fscale(); q.rec_unscale = funscale();
+        q.src_kind = 0; q.ntiles = ntiles;
+        q.t_src_off = t_src_off.as<int>(); q.t_src_k = t_src_k.as<int>();
+        q.t_rec_off = t_rec_off.as<int>(); q.t_rec_r = t_rec_r.as<int>();
         qf = q;
         qk = q;  // drop-in adjoint: the caller's sources, no recording
         qk.rtf_z = qk.rtf_x = nullptr;
@@ -380,6 +448,7 @@ public:
         qa.stf_shot_stride = ntr; qa.stf_ncol = sv.s.nrec; qa.stf_type = sv.s.rtf_type;
         qa.rtf_z = qa.rtf_x = nullptr;
         qa.amp_scale = ascale();
+        qa.src_kind = 1;
         qr = qf;  // recomputed forward: sources and snapshot fix-ups, no recording
         qr.rtf_z = qr.rtf_x = nullptr;
         sp2 = p;  // recompute state: 5 planes per shot and its own CPML strips
@@ -471,11 +540,10 @@ public:
             // forward keeping a state checkpoint at the start of every K-step segment
             for (int it = 0; it < nt; it++) {
                 if (!(it % K)) PSV_TRY(ck_copy(it / K, true));
-                PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
-                PSV_CU(launch_velocity<T>(sp, sv.ns, mode, -1, blk, B, st));
-                PSV_CU(launch_srcrec<T>(sp, qf, it, -1, B, st));
+                PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
+                PSV_CU(launch_velocity<T>(sp, qf, sv.ns, mode, it, -1, rpt, blk, B, st));
             }
-            nk += 3LL * nt;
+            nk += 2LL * nt;
         } else if (ckpt && kind == PASS_ADJ_RES) {
             // segments in reverse: recompute the forward from the checkpoint into
             // the segment snapshot buffer, then the segment's adjoint steps
@@ -485,28 +553,25 @@ public:
                 PSV_TRY(ck_copy(j, false));
                 for (int it = a; it < e; it++) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(launch_stress<T>(sp2, sv.ns, blk, B, st));
-                    PSV_CU(launch_velocity<T>(sp2, sv.ns, MODE_FWD_NOWE, slot, blk, B, st));
-                    PSV_CU(launch_srcrec<T>(sp2, qr, it, slot, B, st));
+                    PSV_CU(launch_stress<T>(sp2, sv.ns, rpt, blk, B, st));
+                    PSV_CU(launch_velocity<T>(sp2, qr, sv.ns, MODE_FWD_NOWE, it, slot, rpt, blk, B, st));
                 }
                 for (int it = e - 1; it >= a; it--) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
-                    PSV_CU(launch_velocity<T>(sp, sv.ns, MODE_ADJ, slot, blk, B, st));
-                    PSV_CU(launch_srcrec<T>(sp, qa, it, -1, B, st));
+                    PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
+                    PSV_CU(launch_velocity<T>(sp, qa, sv.ns, MODE_ADJ, it, slot, rpt, blk, B, st));
                 }
             }
-            nk += 6LL * nt;
+            nk += 4LL * nt;
         } else {
             for (int jt = 0; jt < nt; jt++) {
                 const int it = adj ? nt - 1 - jt : jt;
                 const bool snap = !(it % sdt);
-                PSV_CU(launch_stress<T>(sp, sv.ns, blk, B, st));
-                PSV_CU(launch_velocity<T>(sp, sv.ns, mode, (snap && (store || adj)) ? it / sdt : -1,
-                                          blk, B, st));
-                PSV_CU(launch_srcrec<T>(sp, q, it, (snap && store) ? it / sdt : -1, B, st));
+                PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
+                PSV_CU(launch_velocity<T>(sp, q, sv.ns, mode, it,
+                                          (snap && (store || adj)) ? it / sdt : -1, rpt, blk, B, st));
             }
-            nk += 3LL * nt;
+            nk += 2LL * nt;
         }
         nlaunch = n0 + nk;
         return PSV_OK;
@@ -675,6 +740,7 @@ public:
     {
         if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "gradient: model and observed traces required");
         PSV_TRY(ensure_hist());
+        PSV_TRY(maybe_autotune());
         PSV_TRY(coefficients(true, false));
         const int nshot = sv.s.nshot;
         double tf = 0, ta = 0, to = 0;
@@ -832,23 +898,51 @@ public:
         return PSV_OK;
     }
 
-    int fwi_iteration(double *step, double *L2out, int *ntrials, double *tlog, int maxt) override
+    // copy_mat (n_simulate_PSV.cpp:263): the model the trials and the update start from.
+    int save_model() override
     {
-        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "fwi_iteration: model and observed traces required");
         const size_t n = (size_t)sv.g.nz * sv.g.nx;
-        // copy_mat (n_simulate_PSV.cpp:263)
         PSV_CU(cudaMemcpyAsync(lamc(), lam(), n * 8, cudaMemcpyDeviceToDevice, st));
         PSV_CU(cudaMemcpyAsync(muc(), mu(), n * 8, cudaMemcpyDeviceToDevice, st));
         PSV_CU(cudaMemcpyAsync(rhoc(), rho(), n * 8, cudaMemcpyDeviceToDevice, st));
+        return PSV_OK;
+    }
+
+    // taper2 x3 (n_simulate_PSV.cpp:443-450).
+    int taper_gradient() override
+    {
+        for (int k = 0; k < 3; k++)
+            PSV_CU(launch_taper(grad(k), sv.g.nz, sv.g.nx, taperb.as<double>(),
+                                taperb.as<double>() + sv.g.nx, st));
+        return PSV_OK;
+    }
+
+    // update_mat2 x3 from the saved model (n_simulate_PSV.cpp:542-546).
+    int update_model(double step) override
+    {
+        const int ni = sv.g.nz * sv.g.nx;
+        PSV_CU(launch_update_mat(lam(), lamc(), grad(0), ni, 4.8e+10, 0.0, step, maxbits(), st));
+        PSV_CU(launch_update_mat(mu(), muc(), grad(1), ni, 2.7e+10, 0.0, step, maxbits(), st));
+        PSV_CU(launch_update_mat(rho(), rhoc(), grad(2), ni, 3000.0, 1.25, 0.5 * step, maxbits(), st));
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int trial_misfit(double step, double *L2) override
+    {
+        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "trial: model and observed traces required");
+        return trial(step, L2);
+    }
+
+    int fwi_iteration(double *step, double *L2out, int *ntrials, double *tlog, int maxt) override
+    {
+        if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "fwi_iteration: model and observed traces required");
+        PSV_TRY(save_model());
         double L2 = 0;
         PSV_TRY(gradient(&L2));
         if (L2out) *L2out = L2;
-        const double t_grad = t_ms[0] + t_ms[1] + t_ms[2];
         PSV_CU(cudaEventRecord(ev[0], st));
-        for (int k = 0; k < 3; k++)  // taper2 x3 (:443-450)
-            PSV_CU(launch_taper(grad(k), sv.g.nz, sv.g.nx, taperb.as<double>(),
-                                taperb.as<double>() + sv.g.nx, st));
-
+        PSV_TRY(taper_gradient());
         // step_length_PSV (src/cpu/n_step_length_PSV.cpp:53-209), update_param 0.
         double est = *step;
         auto fn = [](double a, double *L, void *ctx) -> int {
@@ -857,17 +951,12 @@ public:
         const int rc = psv_step_length(&est, L2, fn, this, ntrials, tlog, maxt);
         if (rc != PSV_OK) return rc;
         *step = est;
-        // update_mat2 x3 (n_simulate_PSV.cpp:542-546)
-        const int ni = (int)n;
-        PSV_CU(launch_update_mat(lam(), lamc(), grad(0), ni, 4.8e+10, 0.0, est, maxbits(), st));
-        PSV_CU(launch_update_mat(mu(), muc(), grad(1), ni, 2.7e+10, 0.0, est, maxbits(), st));
-        PSV_CU(launch_update_mat(rho(), rhoc(), grad(2), ni, 3000.0, 1.25, 0.5 * est, maxbits(), st));
+        PSV_TRY(update_model(est));
         PSV_CU(cudaEventRecord(ev[1], st));
         PSV_CU(cudaStreamSynchronize(st));
         float ms = 0;
         PSV_CU(cudaEventElapsedTime(&ms, ev[0], ev[1]));
         t_ms[2] += ms;
-        (void)t_grad;
         return PSV_OK;
     }
 
@@ -875,6 +964,69 @@ public:
     {
         for (int k = 0; k < 3; k++) ms3[k] = t_ms[k];
         return PSV_OK;
+    }
+
+    // Switch the stencil kernels' tile shape (rebuilds the per-tile source
+    // index, drops captured graphs).
+    int set_shape(int r, int by)
+    {
+        r = rpt_ok<T>(r);
+        if (r == rpt && (int)blk.y == by) return PSV_OK;
+        rpt = r;
+        blk = dim3(32, by, 1);
+        PSV_TRY(build_tile_index());
+        qf.t_src_off = qr.t_src_off = qk.t_src_off = qa.t_src_off = t_src_off.as<int>();
+        qf.t_src_k = qr.t_src_k = qk.t_src_k = qa.t_src_k = t_src_k.as<int>();
+        qf.t_rec_off = qr.t_rec_off = qk.t_rec_off = qa.t_rec_off = t_rec_off.as<int>();
+        qf.t_rec_r = qr.t_rec_r = qk.t_rec_r = qa.t_rec_r = t_rec_r.as<int>();
+        qf.ntiles = qr.ntiles = qk.ntiles = qa.ntiles = ntiles;
+        drop_graphs();
+        return PSV_OK;
+    }
+
+    int autotune(int nsteps, int *out_rpt, int *out_by) override
+    {
+        const TuneKey key{sv.g.nz, sv.g.nx, sv.ns, B, (int)sizeof(T), sv.nz2 - sv.nz1};
+        {
+            std::lock_guard<std::mutex> lk(tune_mutex());
+            auto it = tune_cache().find(key);
+            if (it != tune_cache().end()) {
+                PSV_TRY(set_shape(it->second.first, it->second.second));
+                tuned = true;
+                if (out_rpt) *out_rpt = rpt;
+                if (out_by) *out_by = (int)blk.y;
+                return PSV_OK;
+            }
+        }
+        static const int rpts32[] = {1, 2, 4, -2, -4}, rpts64[] = {1};
+        static const int bys[] = {2, 4, 8};
+        const int *rp = sizeof(T) == 8 ? rpts64 : rpts32;
+        const int nr = sizeof(T) == 8 ? 1 : 5;
+        double best = 1e30;
+        int br = rpt, bb = (int)blk.y;
+        for (int i = 0; i < nr; i++)
+            for (int by : bys) {
+                PSV_TRY(set_shape(rp[i], by));
+                double ms[6];
+                PSV_TRY(profile(nsteps, ms));
+                const double t = ms[0] + ms[1] + ms[3] + ms[4];
+                if (t < best) { best = t; br = rpt; bb = by; }
+            }
+        PSV_TRY(set_shape(br, bb));
+        {
+            std::lock_guard<std::mutex> lk(tune_mutex());
+            tune_cache()[key] = {br, bb};
+        }
+        tuned = true;
+        if (out_rpt) *out_rpt = br;
+        if (out_by) *out_by = bb;
+        return PSV_OK;
+    }
+
+    int maybe_autotune()
+    {
+        if (tuned || !opt.autotune || !have_model || !have_obs) return PSV_OK;
+        return autotune(std::min(24, sv.g.nt), nullptr, nullptr);
     }
 
     void *stream() const override { return (void *)st; }
@@ -904,14 +1056,14 @@ public:
                 const int slot = !(it % sdt) ? (it / sdt) % (ckpt ? nslots : sv.snt) : -1;
                 cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
                 cudaEventRecord(E[0], st);
-                cudaError_t c = launch_stress<T>(sp, sv.ns, blk, B, st);
+                cudaError_t c = launch_stress<T>(sp, sv.ns, rpt, blk, B, st);
                 cudaEventRecord(E[1], st);
-                if (c == cudaSuccess) c = launch_velocity<T>(sp, sv.ns, adj ? MODE_ADJ : MODE_FWD, slot, blk, B, st);
+                if (c == cudaSuccess)
+                    c = launch_velocity<T>(sp, q, sv.ns, adj ? MODE_ADJ : MODE_FWD, it, slot, rpt, blk, B, st);
                 cudaEventRecord(E[2], st);
-                if (c == cudaSuccess) c = launch_srcrec<T>(sp, q, it, adj ? -1 : slot, B, st);
                 cudaEventRecord(E[3], st);
                 if (c != cudaSuccess) { rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c)); break; }
-                nlaunch += 3;
+                nlaunch += 2;
             }
         }
         if (rc == PSV_OK) {

@@ -21,7 +21,7 @@ from ._lib import PsvOptions, check, dptr, f64, i32, iptr
 
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
-            block=(0, 0), checkpoint_interval=0) -> PsvOptions:
+            block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True) -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -31,6 +31,8 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.use_graphs = int(bool(use_graphs))
     o.block_x, o.block_y = int(block[0]), int(block[1])
     o.checkpoint_interval = int(checkpoint_interval)
+    o.rows_per_thread = int(rows_per_thread)
+    o.autotune = int(bool(autotune))
     return o
 
 
@@ -134,6 +136,21 @@ class Plan:
         n = nt.value
         return dict(step=st.value, L2=L2.value, ntrials=n, trials=tlog[:min(n, max_trials)].copy())
 
+    # pieces of fwi_iteration, for distributed drivers
+    def save_model(self):
+        check(_lib.lib().psv_save_model(self.h))
+
+    def taper_gradient(self):
+        check(_lib.lib().psv_taper_gradient(self.h))
+
+    def trial_misfit(self, step):
+        L2 = C.c_double()
+        check(_lib.lib().psv_trial_misfit(self.h, float(step), C.byref(L2)))
+        return L2.value
+
+    def update_model(self, step):
+        check(_lib.lib().psv_update_model(self.h, float(step)))
+
     @property
     def stream(self) -> int:
         """cudaStream_t of the plan (for torch.cuda.ExternalStream)."""
@@ -143,11 +160,15 @@ class Plan:
     def kernel_launches(self) -> int:
         return int(_lib.lib().psv_plan_kernel_launches(self.h))
 
+    def autotune(self, nsteps=24):
+        r, b = C.c_int(), C.c_int()
+        check(_lib.lib().psv_plan_autotune(self.h, int(nsteps), C.byref(r), C.byref(b)))
+        return r.value, b.value
+
     def profile_kernels(self, nsteps=100):
         ms = np.zeros(6)
         check(_lib.lib().psv_profile_kernels(self.h, int(nsteps), dptr(ms)))
-        return dict(stress_fwd=ms[0], velocity_fwd=ms[1], srcrec_fwd=ms[2],
-                    stress_adj=ms[3], velocity_adj=ms[4], srcrec_adj=ms[5])
+        return dict(stress_fwd=ms[0], velocity_fwd=ms[1], stress_adj=ms[3], velocity_adj=ms[4])
 
     def timing(self):
         t = np.zeros(3)
@@ -221,7 +242,8 @@ def kernel_PSV(ishot, nt, nz, nx, dt, dx, dz, surf, isurf, hc, fdorder, lam, mu,
     return out
 
 
-def simulate_PSV(workdir: str, max_iter: int = 0, **opts) -> None:
+def simulate_PSV(workdir: str, max_iter: int = 0, imaging_sign: int = -1, **opts) -> None:
     """Run the reference's program (inputs under workdir/bin, workdir/io) on the GPU."""
     o = options(**opts)
-    check(_lib.lib().psv_simulate_PSV(workdir.encode(), int(max_iter), C.byref(o)))
+    check(_lib.lib().psv_simulate_PSV(workdir.encode(), int(max_iter), int(imaging_sign),
+                                      C.byref(o)))

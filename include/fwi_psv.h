@@ -122,7 +122,12 @@ typedef struct psv_options {
     int checkpoint_interval;    /* CHECKPOINT storage: steps per segment, 0 = auto */
     int max_batch;              /* shots per launch; 0 = all shots of the survey */
     int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
-    int block_x, block_y;       /* thread-block shape of the stencil kernels; 0 = tuned */
+    int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
+    int rows_per_thread;        /* rows each thread marches: 1, 2, 4 (negative: warp-shuffle
+                                   variant); 0 = default */
+    int autotune;               /* 1 (default): time the tile-shape candidates on the first
+                                   time loop and keep the fastest (psv_plan_autotune);
+                                   0: use block_y / rows_per_thread as given */
 } psv_options;
 
 void psv_options_default(psv_options *opt);
@@ -231,10 +236,36 @@ int psv_step_length(double *est, double L2_0, psv_trial_fn trial, void *ctx, int
  * past its arrays, include/cpu/n_solvelin.hpp:37-42). */
 double psv_calc_opt_step(const double *L2, const double *sl);
 
+/* The pieces of psv_fwi_iteration, for drivers that split the shots of a
+ * survey over several plans / GPUs and reduce between them:
+ *   psv_save_model      copy_mat: the model trials and the update start from
+ *                       (src/cpu/n_simulate_PSV.cpp:263);
+ *   psv_taper_gradient  taper2 of the three global gradients (:443-450);
+ *   psv_trial_misfit    one trial of step_length_PSV: update_mat2 of the saved
+ *                       model by `step` (rho by step/2, floor 1.5), forward of
+ *                       this plan's shots, their summed L2
+ *                       (src/cpu/n_step_length_PSV.cpp:87-123);
+ *   psv_update_model    the final update_mat2 x3 (:542-546).
+ * A distributed iteration: save, gradient, all-reduce the gradients and L2,
+ * psv_set_gradient, taper, psv_step_length with trials whose L2 is
+ * all-reduced, update. */
+int psv_save_model(psv_plan *plan);
+int psv_taper_gradient(psv_plan *plan);
+int psv_trial_misfit(psv_plan *plan, double step, double *L2);
+int psv_update_model(psv_plan *plan, double step);
+
 /* Event-timed device milliseconds of the last forward / gradient /
  * iteration call, split: [0] forward, [1] adjoint (incl. recompute), [2]
  * everything else. */
 int psv_last_timing(const psv_plan *plan, double *ms3);
+
+/* Tile-shape autotuner: times every (rows per thread, block height)
+ * candidate of the stencil kernels over nsteps forward + nsteps adjoint
+ * steps (CUDA events) and keeps the fastest.  Results are cached per
+ * (grid, stencil order, batch, precision) for the process.  Needs a model
+ * and observed traces (it runs the kernels on them); leaves the wavefields
+ * undefined.  Outputs the chosen shape. */
+int psv_plan_autotune(psv_plan *plan, int nsteps, int *rows_per_thread, int *block_y);
 
 /* The CUDA stream every call of this plan runs on (a cudaStream_t), for
  * callers that time or order work against it. */
@@ -245,7 +276,8 @@ long long psv_plan_kernel_launches(const psv_plan *plan);
 /* Event-timed profile of the time-step kernels: nsteps forward steps then
  * nsteps adjoint steps of the first batch, each kernel bracketed by CUDA
  * events on the plan's stream.  ms6 = mean milliseconds per launch of
- * {stress, velocity, source/receiver} forward, then the same adjoint.
+ * {stress, velocity, 0} forward, then the same adjoint (sources and
+ * receivers run inside the velocity kernel; slots 2 and 5 stay 0).
  * Needs a model and observed traces; leaves the wavefields undefined. */
 int psv_profile_kernels(psv_plan *plan, int nsteps, double *ms6);
 
@@ -293,8 +325,10 @@ int psv_kernel_PSV(int ishot, int nt, int nz, int nx, double dt, double dx, doub
  * bin/shot{i}_rtf_u{z,x}.bin and, with accu_save, bin/shot{i}_{vz,vx,szz,szx,sxx}.bin)
  * or FWI (writing bin/iter{n}_mat.bin every mat_save_interval iterations).
  * max_iter caps the FWI iterations (the reference's cap is 1000 with an
- * early stop after 25, src/cpu/n_simulate_PSV.cpp:240,576-581; 0 = that). */
-int psv_simulate_PSV(const char *workdir, int max_iter, const psv_options *opt);
+ * early stop after 25, src/cpu/n_simulate_PSV.cpp:240,576-581; 0 = that).
+ * imaging_sign has the meaning of the grid field of that name (the files
+ * carry no such field; <= 0 is the reference's CPU path). */
+int psv_simulate_PSV(const char *workdir, int max_iter, int imaging_sign, const psv_options *opt);
 
 #ifdef __cplusplus
 }

@@ -80,6 +80,28 @@ def main():
     out[f"{name}/obs_uz"], out[f"{name}/obs_ux"] = uz, ux
     for k in ("L2", "step", "lam", "mu", "rho", "grad_lam", "grad_mu", "grad_rho"):
         out[f"{name}/{k}"] = r[k]
+    # whole program: the reference's simulate_PSV() on its binary inputs
+    # (forward modelling with snapshot and seismogram output)
+    import tempfile
+    from fwi_cuda_gb300 import io as fio
+    sv, true, _ = helpers.crosswell(nt=200, nz=45, nx=37, nshot=2, nrec=10, npml=8, snap_dt=5)
+    sv.snap_dz = sv.snap_dx = 3
+    work = tempfile.mkdtemp()
+    fio.write_inputs(work, sv, *true, fwinv=False, accu_save=True, seismo_save=True, gpu_code=False)
+    name = "program_fwd"
+    for f in ("metaint", "intarray", "metafloat", "mat"):
+        out[f"{name}/{f}.bin"] = np.fromfile(os.path.join(work, "bin", f + ".bin"), np.uint8)
+    assert ref.lib.ref_simulate_PSV_in_dir(work.encode()) == 0
+    snt, snz, snx = sv.snap_dims()
+    for s in range(sv.nshot):
+        uz, ux = fio.read_seismo(work, s, sv.nrec, sv.nt)
+        out[f"{name}/shot{s}_rtf_uz"], out[f"{name}/shot{s}_rtf_ux"] = uz, ux
+        acc = fio.read_accu(work, s, (snt, snz, snx))
+        for k in ("vz", "szx"):
+            out[f"{name}/shot{s}_{k}"] = acc[k]
+    pack(name, sv, out)
+    out[f"{name}/model"] = np.stack(true)
+
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_cases.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path))
