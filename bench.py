@@ -183,13 +183,21 @@ def run_profile(args):
     nt / shots from --nt / --nshot; prints nothing measured."""
     from fwi_cuda_gb300 import engine
     sv, true, init = workload(nt=args.nt, nshot=args.nshot)
-    with engine.Plan(sv, precision=32) as p:
+    with engine.Plan(sv, precision=32, **plan_kernels(args)) as p:
         p.set_model(*true)
         obs = p.forward()
         p.set_model(*init)
         p.set_observed(*obs)
         L2, _ = p.gradient(fetch=False)
-    print(json.dumps({"profile_case": {"nt": sv.nt, "nshot": sv.nshot, "L2": L2}}))
+    print(json.dumps({"profile_case": {"nt": sv.nt, "nshot": sv.nshot, "L2": L2,
+                                       "kernels": args.kernels, "rows_per_thread": args.rpt}}))
+
+
+def plan_kernels(args):
+    """Plan options for --kernels / --rpt (auto: the autotuner chooses)."""
+    if args.kernels == "auto":
+        return {}
+    return dict(kernels=args.kernels, rows_per_thread=args.rpt or (4 if args.kernels == "tma" else 1))
 
 
 def run_ours(args, rank, world):
@@ -200,11 +208,13 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     sv, true, init = workload()
     nt, nshot = sv.nt, sv.nshot
-    with engine.Plan(sv, precision=32) as p:
+    with engine.Plan(sv, precision=32, **plan_kernels(args)) as p:
         p.set_model(*true)
         obs_uz, obs_ux = p.forward()          # observed data from the true model
         p.set_model(*init)
         p.set_observed(obs_uz, obs_ux)
+        fam, rpt, by = p.autotune() if args.kernels == "auto" else (args.kernels, 0, 0)
+        kernels = {"family": fam, "rows_per_thread": rpt, "block_y": by}
         stream = torch.cuda.ExternalStream(p.stream)
         flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 
@@ -292,7 +302,7 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded layered model)",
-        "config": config_dict(world),
+        "config": config_dict(world, {"kernels": kernels}),
         "shots_per_s": nshot * world / (ms / 1e3),
         "split_ms": {k: round(v, 3) for k, v in split.items()},
         "e2e": {"value": updates_per_step(nt, nshot) * world / e2e_s, "unit": UNIT,
@@ -337,6 +347,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--kernels", choices=["auto", "direct", "tma"], default="auto",
+                    help="time-step kernel family (auto: the plan's autotuner picks)")
+    ap.add_argument("--rpt", type=int, default=0, help="rows per thread with --kernels")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-nt", type=int, default=1000)
     ap.add_argument("--ref-nt", type=int, default=400)

@@ -60,7 +60,7 @@ class PsvOptions(C.Structure):
         ("precision", C.c_int), ("storage", C.c_int), ("hbm_budget_gb", C.c_double),
         ("checkpoint_interval", C.c_int), ("max_batch", C.c_int), ("use_graphs", C.c_int),
         ("block_x", C.c_int), ("block_y", C.c_int), ("rows_per_thread", C.c_int),
-        ("autotune", C.c_int),
+        ("kernel_family", C.c_int), ("autotune", C.c_int),
     ]
 
 
@@ -100,7 +100,8 @@ SIGNATURES = {
     "psv_plan_stream": (C.c_void_p, [C.c_void_p]),
     "psv_plan_kernel_launches": (C.c_longlong, [C.c_void_p]),
     "psv_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, _dp]),
-    "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
+    "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip]),
+    "psv_plan_shape": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
     "psv_step_length": (C.c_int, [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp, C.c_int]),
     "psv_calc_opt_step": (C.c_double, [_dp, _dp]),
     "psv_kernel_PSV": (C.c_int,

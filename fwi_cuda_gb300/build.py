@@ -30,6 +30,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-u
 UNITS = [
     ("psv_kernels_f32.cu", []),
     ("psv_kernels_f64.cu", []),
+    ("psv_tiled.cu", []),
     ("psv_fwi_kernels.cu", ["-fmad=false"]),
     ("psv_plan_f32.cu", []),
     ("psv_plan_f64.cu", []),

@@ -303,10 +303,18 @@ void *psv_plan_stream(const psv_plan *p) { return p && p->impl ? p->impl->stream
 
 long long psv_plan_kernel_launches(const psv_plan *p) { return p && p->impl ? p->impl->launches() : 0; }
 
-int psv_plan_autotune(psv_plan *p, int nsteps, int *rpt, int *by)
+int psv_plan_autotune(psv_plan *p, int nsteps, int *family, int *rpt, int *by)
 {
     PLAN_CHECK(p);
-    return p->impl->autotune(nsteps, rpt, by);
+    if (nsteps <= 0) return fail(PSV_ERR_ARG, "autotune: nsteps must be positive");
+    return p->impl->autotune(nsteps, family, rpt, by);
+}
+
+int psv_plan_shape(const psv_plan *p, int *family, int *rpt, int *by)
+{
+    PLAN_CHECK(p);
+    p->impl->shape(family, rpt, by);
+    return PSV_OK;
 }
 
 int psv_profile_kernels(psv_plan *p, int nsteps, double *ms6)

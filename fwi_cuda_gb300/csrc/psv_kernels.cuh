@@ -64,6 +64,7 @@ struct StepParams {
     T *gshot;                  // [batch][3][snz][snx_pitch] (grad_lam, grad_mu, grad_rho)
     long long gshot_shot_stride;
     const int *ctl;            // device [2]: global index of batch shot 0, shots in this batch
+    int *err;                  // device error word (nonzero: a bounded wait gave up)
 };
 
 // Source injection and receiver recording of one step for every shot of a batch.

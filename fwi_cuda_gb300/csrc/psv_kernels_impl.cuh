@@ -36,288 +36,202 @@ __device__ __forceinline__ T xnb(T own, int d, const T *__restrict__ row, int ix
 }
 
 // ---------------------------------------------------------------------------
-// Stress step: vdiff2 + pml_diff2 + update_s2 + surf_mirror
-// (src/cpu/n_kernel_lib_PSV.cpp:100-131, 134-178, 181-205, 272-395).
-//
-// Interior points only.  The free-surface mirror is done by the thread that
-// owns the image row/column: it writes the negated new stress to the mirrored
-// cell, while the mirrored cell's own thread skips writing the mirrored
-// components.  Every cell has exactly one writer and the result equals the
-// reference's update-then-mirror sequence for a top and/or bottom surface, or
-// a left and/or right surface.
+// Per-point pieces shared by the direct-load kernels below and the TMA tile
+// kernels (psv_tiled.cu), so both compute the same floating-point operations.
 // ---------------------------------------------------------------------------
-template <typename T, int NS, int RPT, bool SH>
-__global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
+
+// pml_diff2 on the velocity derivatives of a stress update
+// (src/cpu/n_kernel_lib_PSV.cpp:134-178), only on the absorbing strips
+// (a = 0, b = K = 1 elsewhere).
+template <typename T>
+__device__ __forceinline__ void cpml_stress(const StepParams<T> &p, int shot, int iz, int ix,
+                                            T &vz_z, T &vx_z, T &vz_x, T &vx_x)
 {
-    if ((int)blockIdx.z >= p.ctl[1]) return;
-    const int ix = p.nx1 + blockIdx.x * 32 + threadIdx.x;
-    const int zb = p.nz1 + (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
-    if (zb >= p.nz2) return;  // uniform across the warp; no block barrier follows
-    const long long P = p.pitch;
-    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
-    const T *__restrict__ vz = f + F_VZ * p.plane;
-    const T *__restrict__ vx = f + F_VX * p.plane;
-    T *szz = f + F_SZZ * p.plane;
-    T *szx = f + F_SZX * p.plane;
-    T *sxx = f + F_SXX * p.plane;
-    const bool colin = ix < p.nx2, colok = ix < p.nx;
-
-    // wz[j] = vz[zb - N + j], wx[j] = vx[zb - N + 1 + j]
-    constexpr int W = RPT + 2 * NS - 1;
-    T wz[W], wx[W];
-#pragma unroll
-    for (int j = 0; j < W; j++) {
-        const int rz = zb - NS + j, rx = zb - NS + 1 + j;  // >= 0: zb >= fpad >= N
-        wz[j] = (colok && rz < p.nz) ? vz[(long long)rz * P + ix] : T(0);
-        wx[j] = (colok && rx < p.nz) ? vx[(long long)rx * P + ix] : T(0);
+    if (iz < p.pz0 || iz >= p.pz1) {
+        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
+        T *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
+        const T m0 = p.b_z[iz] * m[MZ_VZ * p.mz_plane] + p.a_z[iz] * vz_z;
+        const T m1 = p.bh_z[iz] * m[MZ_VX * p.mz_plane] + p.ah_z[iz] * vx_z;
+        m[MZ_VZ * p.mz_plane] = m0;
+        m[MZ_VX * p.mz_plane] = m1;
+        vz_z = vz_z * p.ki_z[iz] + m0;
+        vx_z = vx_z * p.khi_z[iz] + m1;
     }
-
-#pragma unroll
-    for (int r = 0; r < RPT; r++) {
-        const int iz = zb + r;
-        const bool rowload = iz < p.nz;
-        const long long rowoff = (long long)(rowload ? iz : 0) * P;
-        const T *vzr = vz + rowoff, *vxr = vx + rowoff;
-        // staggered derivatives; term 1 is the reference's 2-point difference
-        const T oz = wz[r + NS], ox = wx[r + NS - 1];
-        T vz_z = p.cz[0] * (oz - wz[r + NS - 1]);
-        T vx_z = p.cz[0] * (wx[r + NS] - ox);
-        T vz_x = p.cx[0] * (xnb<SH>(oz, 1, vzr, ix, p.nx, rowload) - oz);
-        T vx_x = p.cx[0] * (ox - xnb<SH>(ox, -1, vxr, ix, p.nx, rowload));
-#pragma unroll
-        for (int k = 2; k <= NS; k++) {
-            vz_z += p.cz[k - 1] * (wz[r + NS + k - 1] - wz[r + NS - k]);
-            vx_z += p.cz[k - 1] * (wx[r + NS + k - 1] - wx[r + NS - k]);
-            vz_x += p.cx[k - 1] * (xnb<SH>(oz, k, vzr, ix, p.nx, rowload) -
-                                   xnb<SH>(oz, -(k - 1), vzr, ix, p.nx, rowload));
-            vx_x += p.cx[k - 1] * (xnb<SH>(ox, k - 1, vxr, ix, p.nx, rowload) -
-                                   xnb<SH>(ox, -k, vxr, ix, p.nx, rowload));
-        }
-        if (iz >= p.nz2 || !colin) continue;
-        const long long i = (long long)iz * P + ix;
-
-        // CPML recursion, only on the absorbing strips (a = 0, b = K = 1 elsewhere)
-        if (iz < p.pz0 || iz >= p.pz1) {
-            const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-            T *m = p.memz + (long long)blockIdx.z * p.mz_shot_stride + (long long)rr * P + ix;
-            const T m0 = p.b_z[iz] * m[MZ_VZ * p.mz_plane] + p.a_z[iz] * vz_z;
-            const T m1 = p.bh_z[iz] * m[MZ_VX * p.mz_plane] + p.ah_z[iz] * vx_z;
-            m[MZ_VZ * p.mz_plane] = m0;
-            m[MZ_VX * p.mz_plane] = m1;
-            vz_z = vz_z * p.ki_z[iz] + m0;
-            vx_z = vx_z * p.khi_z[iz] + m1;
-        }
-        if (ix < p.px0 || ix >= p.px1) {
-            const int c = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-            T *m = p.memx + (long long)blockIdx.z * p.mx_shot_stride + (long long)iz * p.mx_pitch + c;
-            const T m0 = p.b_x[ix] * m[MX_VX * p.mx_plane] + p.a_x[ix] * vx_x;
-            const T m1 = p.bh_x[ix] * m[MX_VZ * p.mx_plane] + p.ah_x[ix] * vz_x;
-            m[MX_VX * p.mx_plane] = m0;
-            m[MX_VZ * p.mx_plane] = m1;
-            vx_x = vx_x * p.ki_x[ix] + m0;
-            vz_x = vz_x * p.khi_x[ix] + m1;
-        }
-
-        const T cl = p.c_lam[i], c2 = p.c_l2m[i];
-        T nzz = szz[i] + (c2 * vz_z + cl * vx_x);
-        T nxx = sxx[i] + (cl * vz_z + c2 * vx_x);
-        T nzx = szx[i] + p.c_muzx[i] * (vz_x + vx_z);
-
-        bool wzz = true, wzx = true, wxx = true;
-        if (p.st) {  // top: rows [nz1, st) mirror rows (st, 2 st - nz1]
-            if (iz == p.st) {
-                nzz = T(0); nzx = T(0);
-                nxx = p.fs_top[ix] * vx_x;
-            } else if (iz < p.st) {
-                wzz = false; wzx = false;
-            } else if (iz <= 2 * p.st - p.nz1) {
-                const long long j = (long long)(2 * p.st - iz) * P + ix;
-                szz[j] = -nzz; szx[j] = -nzx;
-            }
-        }
-        if (p.sb) {  // bottom: rows (sb, nz2] mirror rows [2 sb - nz2, sb)
-            if (iz == p.sb) {
-                nzz = T(0); nzx = T(0);
-                nxx = p.fs_bot[ix] * vx_x;
-            } else if (iz > p.sb) {
-                wzz = false; wzx = false;
-            } else if (iz >= 2 * p.sb - p.nz2) {
-                const long long j = (long long)(2 * p.sb - iz) * P + ix;
-                szz[j] = -nzz; szx[j] = -nzx;
-            }
-        }
-        if (p.sl) {  // left: columns [nx1, sl) mirror columns (sl, 2 sl - nx1]
-            if (ix == p.sl) {
-                nxx = T(0); nzx = T(0);
-                nzz = p.fs_left[iz] * vz_z;
-            } else if (ix < p.sl) {
-                wzx = false; wxx = false;
-            } else if (ix <= 2 * p.sl - p.nx1) {
-                const long long j = (long long)iz * P + (2 * p.sl - ix);
-                szx[j] = -nzx; sxx[j] = -nxx;
-            }
-        }
-        if (p.sr) {  // right: columns (sr, nx2] mirror columns [2 sr - nx2, sr)
-            if (ix == p.sr) {
-                nxx = T(0); nzx = T(0);
-                nzz = p.fs_right[iz] * vz_z;
-            } else if (ix > p.sr) {
-                wzx = false; wxx = false;
-            } else if (ix >= 2 * p.sr - p.nx2) {
-                const long long j = (long long)iz * P + (2 * p.sr - ix);
-                szx[j] = -nzx; sxx[j] = -nxx;
-            }
-        }
-        if (wzz) szz[i] = nzz;
-        if (wzx) szx[i] = nzx;
-        if (wxx) sxx[i] = nxx;
+    if (ix < p.px0 || ix >= p.px1) {
+        const int c = ix < p.px0 ? ix : ix - p.px1 + p.px0;
+        T *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + c;
+        const T m0 = p.b_x[ix] * m[MX_VX * p.mx_plane] + p.a_x[ix] * vx_x;
+        const T m1 = p.bh_x[ix] * m[MX_VZ * p.mx_plane] + p.ah_x[ix] * vz_x;
+        m[MX_VX * p.mx_plane] = m0;
+        m[MX_VZ * p.mx_plane] = m1;
+        vx_x = vx_x * p.ki_x[ix] + m0;
+        vz_x = vz_x * p.khi_x[ix] + m1;
     }
 }
 
-// ---------------------------------------------------------------------------
-// Velocity step: sdiff2 + pml_diff2 + update_v2 (src/cpu/n_kernel_lib_PSV.cpp:
-// 207-270, 134-178), fused with the step's remaining work:
-//   forward modes: gard_fwd_storage2 (:398-436) into `slot`;
-//   MODE_ADJ: u += dt v, and fwi_grad2 (:439-484, CPU sign) against `slot`;
-//   epilogue: vsrc2 + urec2 (:487-576) for the sources / receivers of the
-//   block's tile, after all of the tile's velocities are written.
-// Covers the whole grid: cells outside the interior only take part in the
-// snapshot / imaging work (their fields are never updated).
-// ---------------------------------------------------------------------------
-template <typename T, int NS, int MODE, int RPT, bool SH>
-__global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const SrcRecParams<T> q,
-                                                  const int it, const int slot)
+// update_s2 + surf_mirror (src/cpu/n_kernel_lib_PSV.cpp:181-205, 272-395) of
+// interior point (iz, ix) from its old stresses o*, the dt-scaled
+// coefficients and the (CPML-corrected) derivatives.  The thread that owns
+// an image row/column writes the negated new stress into the mirrored cell;
+// the mirrored cell's own thread skips those components, so every cell has
+// one writer and the result equals the reference's update-then-mirror
+// sequence for a top and/or bottom surface, or a left and/or right surface.
+template <typename T>
+__device__ __forceinline__ void stress_finish(const StepParams<T> &p, T *szz, T *szx, T *sxx,
+                                              int iz, int ix, long long i, T ozz, T ozx, T oxx,
+                                              T cl, T c2, T cm, T vz_z, T vx_z, T vz_x, T vx_x)
 {
-    if ((int)blockIdx.z >= p.ctl[1]) return;  // whole block
-    const int ix = blockIdx.x * 32 + threadIdx.x;
-    const int zb = (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
     const long long P = p.pitch;
-    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
-    const T *__restrict__ szz = f + F_SZZ * p.plane;
-    const T *__restrict__ szx = f + F_SZX * p.plane;
-    const T *__restrict__ sxx = f + F_SXX * p.plane;
-    T *vz = f + F_VZ * p.plane;
-    T *vx = f + F_VX * p.plane;
-    const bool colok = ix < p.nx;
-    const bool colin = ix >= p.nx1 && ix < p.nx2;
-    const long long sp = p.snap_plane;
-
-    if (zb < p.nz) {  // warp-uniform
-        // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
-        constexpr int W = RPT + 2 * NS - 1;
-        T wzz[W], wzx[W], wxx[RPT];
-#pragma unroll
-        for (int j = 0; j < W; j++) {
-            const int ra = zb - NS + 1 + j, rb = zb - NS + j;
-            wzz[j] = (colok && ra >= 0 && ra < p.nz) ? szz[(long long)ra * P + ix] : T(0);
-            wzx[j] = (colok && rb >= 0 && rb < p.nz) ? szx[(long long)rb * P + ix] : T(0);
-        }
-#pragma unroll
-        for (int r = 0; r < RPT; r++) {
-            const int iz = zb + r;
-            wxx[r] = (colok && iz < p.nz) ? sxx[(long long)iz * P + ix] : T(0);
-        }
-
-#pragma unroll
-        for (int r = 0; r < RPT; r++) {
-            const int iz = zb + r;
-            const bool rowload = iz < p.nz;
-            const long long rowoff = (long long)(rowload ? iz : 0) * P;
-            const T *szxr = szx + rowoff, *sxxr = sxx + rowoff;
-            const T ozz = wzz[r + NS - 1], ozx = wzx[r + NS], oxx = wxx[r];
-            T szz_z = p.cz[0] * (wzz[r + NS] - ozz);
-            T szx_z = p.cz[0] * (ozx - wzx[r + NS - 1]);
-            T szx_x = p.cx[0] * (ozx - xnb<SH>(ozx, -1, szxr, ix, p.nx, rowload));
-            T sxx_x = p.cx[0] * (xnb<SH>(oxx, 1, sxxr, ix, p.nx, rowload) - oxx);
-#pragma unroll
-            for (int k = 2; k <= NS; k++) {
-                szz_z += p.cz[k - 1] * (wzz[r + NS + k - 1] - wzz[r + NS - k]);
-                szx_z += p.cz[k - 1] * (wzx[r + NS + k - 1] - wzx[r + NS - k]);
-                szx_x += p.cx[k - 1] * (xnb<SH>(ozx, k - 1, szxr, ix, p.nx, rowload) -
-                                        xnb<SH>(ozx, -k, szxr, ix, p.nx, rowload));
-                sxx_x += p.cx[k - 1] * (xnb<SH>(oxx, k, sxxr, ix, p.nx, rowload) -
-                                        xnb<SH>(oxx, -(k - 1), sxxr, ix, p.nx, rowload));
-            }
-            if (!rowload || !colok) continue;
-            const long long i = (long long)iz * P + ix;
-            const bool inner = colin && iz >= p.nz1 && iz < p.nz2;
-            T vzn, vxn, uzn = T(0), uxn = T(0);
-            if (inner) {
-                if (iz < p.pz0 || iz >= p.pz1) {
-                    const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-                    T *m = p.memz + (long long)blockIdx.z * p.mz_shot_stride + (long long)rr * P + ix;
-                    const T m0 = p.b_z[iz] * m[MZ_SZZ * p.mz_plane] + p.a_z[iz] * szz_z;
-                    const T m1 = p.bh_z[iz] * m[MZ_SZX * p.mz_plane] + p.ah_z[iz] * szx_z;
-                    m[MZ_SZZ * p.mz_plane] = m0;
-                    m[MZ_SZX * p.mz_plane] = m1;
-                    szz_z = szz_z * p.ki_z[iz] + m0;
-                    szx_z = szx_z * p.khi_z[iz] + m1;
-                }
-                if (ix < p.px0 || ix >= p.px1) {
-                    const int c = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-                    T *m = p.memx + (long long)blockIdx.z * p.mx_shot_stride + (long long)iz * p.mx_pitch + c;
-                    const T m0 = p.b_x[ix] * m[MX_SXX * p.mx_plane] + p.a_x[ix] * sxx_x;
-                    const T m1 = p.bh_x[ix] * m[MX_SZX * p.mx_plane] + p.ah_x[ix] * szx_x;
-                    m[MX_SXX * p.mx_plane] = m0;
-                    m[MX_SZX * p.mx_plane] = m1;
-                    sxx_x = sxx_x * p.ki_x[ix] + m0;
-                    szx_x = szx_x * p.khi_x[ix] + m1;
-                }
-                const T vzo = vz[i], vxo = vx[i];
-                if (MODE == MODE_ADJ || MODE == MODE_FWD_U) {
-                    T *uz = f + F_UZ * p.plane;
-                    T *ux = f + F_UX * p.plane;
-                    uzn = uz[i] + p.dt * vzo;
-                    uxn = ux[i] + p.dt * vxo;
-                    uz[i] = uzn;
-                    ux[i] = uxn;
-                }
-                vzn = vzo + p.c_rz[i] * (szx_x + szz_z);
-                vxn = vxo + p.c_rx[i] * (sxx_x + szx_z);
-                vz[i] = vzn;
-                vx[i] = vxn;
-                if (MODE != MODE_FWD_NOWE) {
-                    T *we = f + (MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane;
-                    we[i] += vxn * vxn + vzn * vzn;
-                }
-            } else {
-                vzn = vz[i];
-                vxn = vx[i];
-                if (MODE == MODE_ADJ || MODE == MODE_FWD_U) {
-                    uzn = f[F_UZ * p.plane + i];
-                    uxn = f[F_UX * p.plane + i];
-                }
-            }
-            if (slot < 0) continue;
-            const int dzr = iz - p.snap_z1, dxr = ix - p.snap_x1;
-            if (dzr < 0 || iz > p.snap_z2 || dxr < 0 || ix > p.snap_x2) continue;
-            if (dzr % p.snap_dz || dxr % p.snap_dx) continue;
-            const long long qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
-            T *h = p.hist + (long long)blockIdx.z * p.hist_shot_stride + (long long)slot * p.hist_slot_stride + qq;
-            if (MODE != MODE_ADJ) {
-                h[H_SZZ * sp] = ozz;
-                h[H_SZX * sp] = ozx;
-                h[H_SXX * sp] = oxx;
-                h[H_VZ * sp] = vzn * p.inv_dt;
-                h[H_VX * sp] = vxn * p.inv_dt;
-            } else {
-                const T fzz = h[H_SZZ * sp], fzx = h[H_SZX * sp], fxx = h[H_SXX * sp];
-                const T fvz = h[H_VZ * sp], fvx = h[H_VX * sp];
-                const T s1 = p.g1[i] * ((fzz + fxx) * (ozz + oxx));
-                const T s23 = p.g2[i] * (fzx * ozx + T(0.25) * ((fzz - fxx) * (ozz - oxx)));
-                T *g = p.gshot + (long long)blockIdx.z * p.gshot_shot_stride + qq;
-                g[0] -= s1;
-                g[sp] -= s23 + s1;
-                g[2 * sp] -= p.kimg * (uxn * fvx + uzn * fvz);
-            }
+    T nzz = ozz + (c2 * vz_z + cl * vx_x);
+    T nxx = oxx + (cl * vz_z + c2 * vx_x);
+    T nzx = ozx + cm * (vz_x + vx_z);
+    bool wzz = true, wzx = true, wxx = true;
+    if (p.st) {  // top: rows [nz1, st) mirror rows (st, 2 st - nz1]
+        if (iz == p.st) {
+            nzz = T(0); nzx = T(0);
+            nxx = p.fs_top[ix] * vx_x;
+        } else if (iz < p.st) {
+            wzz = false; wzx = false;
+        } else if (iz <= 2 * p.st - p.nz1) {
+            const long long j = (long long)(2 * p.st - iz) * P + ix;
+            szz[j] = -nzz; szx[j] = -nzx;
         }
     }
+    if (p.sb) {  // bottom: rows (sb, nz2] mirror rows [2 sb - nz2, sb)
+        if (iz == p.sb) {
+            nzz = T(0); nzx = T(0);
+            nxx = p.fs_bot[ix] * vx_x;
+        } else if (iz > p.sb) {
+            wzz = false; wzx = false;
+        } else if (iz >= 2 * p.sb - p.nz2) {
+            const long long j = (long long)(2 * p.sb - iz) * P + ix;
+            szz[j] = -nzz; szx[j] = -nzx;
+        }
+    }
+    if (p.sl) {  // left: columns [nx1, sl) mirror columns (sl, 2 sl - nx1]
+        if (ix == p.sl) {
+            nxx = T(0); nzx = T(0);
+            nzz = p.fs_left[iz] * vz_z;
+        } else if (ix < p.sl) {
+            wzx = false; wxx = false;
+        } else if (ix <= 2 * p.sl - p.nx1) {
+            const long long j = (long long)iz * P + (2 * p.sl - ix);
+            szx[j] = -nzx; sxx[j] = -nxx;
+        }
+    }
+    if (p.sr) {  // right: columns (sr, nx2] mirror columns [2 sr - nx2, sr)
+        if (ix == p.sr) {
+            nxx = T(0); nzx = T(0);
+            nzz = p.fs_right[iz] * vz_z;
+        } else if (ix > p.sr) {
+            wzx = false; wxx = false;
+        } else if (ix >= 2 * p.sr - p.nx2) {
+            const long long j = (long long)iz * P + (2 * p.sr - ix);
+            szx[j] = -nzx; sxx[j] = -nxx;
+        }
+    }
+    if (wzz) szz[i] = nzz;
+    if (wzx) szx[i] = nzx;
+    if (wxx) sxx[i] = nxx;
+}
 
-    // ---- epilogue: sources and receivers of this tile (vsrc2, urec2) ----
+// pml_diff2 on the stress derivatives of a velocity update.
+template <typename T>
+__device__ __forceinline__ void cpml_velocity(const StepParams<T> &p, int shot, int iz, int ix,
+                                              T &szz_z, T &szx_z, T &szx_x, T &sxx_x)
+{
+    if (iz < p.pz0 || iz >= p.pz1) {
+        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
+        T *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
+        const T m0 = p.b_z[iz] * m[MZ_SZZ * p.mz_plane] + p.a_z[iz] * szz_z;
+        const T m1 = p.bh_z[iz] * m[MZ_SZX * p.mz_plane] + p.ah_z[iz] * szx_z;
+        m[MZ_SZZ * p.mz_plane] = m0;
+        m[MZ_SZX * p.mz_plane] = m1;
+        szz_z = szz_z * p.ki_z[iz] + m0;
+        szx_z = szx_z * p.khi_z[iz] + m1;
+    }
+    if (ix < p.px0 || ix >= p.px1) {
+        const int c = ix < p.px0 ? ix : ix - p.px1 + p.px0;
+        T *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + c;
+        const T m0 = p.b_x[ix] * m[MX_SXX * p.mx_plane] + p.a_x[ix] * sxx_x;
+        const T m1 = p.bh_x[ix] * m[MX_SZX * p.mx_plane] + p.ah_x[ix] * szx_x;
+        m[MX_SXX * p.mx_plane] = m0;
+        m[MX_SZX * p.mx_plane] = m1;
+        sxx_x = sxx_x * p.ki_x[ix] + m0;
+        szx_x = szx_x * p.khi_x[ix] + m1;
+    }
+}
+
+// gard_fwd_storage2 (forward: store the step's snapshot into `slot`) or
+// fwi_grad2 (adjoint: image against snapshot `slot`, CPU sign) at point
+// (iz, ix) of the snapshot window (src/cpu/n_kernel_lib_PSV.cpp:398-484).
+template <typename T, int MODE>
+__device__ __forceinline__ void snapshot_point(const StepParams<T> &p, int shot, int iz, int ix,
+                                               long long i, int slot, T ozz, T ozx, T oxx, T vzn,
+                                               T vxn, T uzn, T uxn)
+{
+    const int dzr = iz - p.snap_z1, dxr = ix - p.snap_x1;
+    if (dzr < 0 || iz > p.snap_z2 || dxr < 0 || ix > p.snap_x2) return;
+    if (dzr % p.snap_dz || dxr % p.snap_dx) return;
+    const long long sp = p.snap_plane;
+    const long long qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
+    T *h = p.hist + (long long)shot * p.hist_shot_stride + (long long)slot * p.hist_slot_stride + qq;
+    if (MODE != MODE_ADJ) {
+        h[H_SZZ * sp] = ozz;
+        h[H_SZX * sp] = ozx;
+        h[H_SXX * sp] = oxx;
+        h[H_VZ * sp] = vzn * p.inv_dt;
+        h[H_VX * sp] = vxn * p.inv_dt;
+    } else {
+        const T fzz = h[H_SZZ * sp], fzx = h[H_SZX * sp], fxx = h[H_SXX * sp];
+        const T fvz = h[H_VZ * sp], fvx = h[H_VX * sp];
+        const T s1 = p.g1[i] * ((fzz + fxx) * (ozz + oxx));
+        const T s23 = p.g2[i] * (fzx * ozx + T(0.25) * ((fzz - fxx) * (ozz - oxx)));
+        T *g = p.gshot + (long long)shot * p.gshot_shot_stride + qq;
+        g[0] -= s1;
+        g[sp] -= s23 + s1;
+        g[2 * sp] -= p.kimg * (uxn * fvx + uzn * fvz);
+    }
+}
+
+// update_v2 (src/cpu/n_kernel_lib_PSV.cpp:243-270) of interior point i from
+// its old velocities, plus the displacement integration (adjoint and the
+// drop-in forward) and the energy sum We / We_adj from the old u / We
+// values; stores and returns the new values.
+template <typename T, int MODE>
+__device__ __forceinline__ void velocity_finish(const StepParams<T> &p, T *f, long long i, T vzo,
+                                                T vxo, T uzo, T uxo, T weo, T crz, T crx,
+                                                T szz_z, T szx_z, T szx_x, T sxx_x, T &vzn,
+                                                T &vxn, T &uzn, T &uxn)
+{
+    if (MODE == MODE_ADJ || MODE == MODE_FWD_U) {
+        uzn = uzo + p.dt * vzo;
+        uxn = uxo + p.dt * vxo;
+        f[F_UZ * p.plane + i] = uzn;
+        f[F_UX * p.plane + i] = uxn;
+    }
+    vzn = vzo + crz * (szx_x + szz_z);
+    vxn = vxo + crx * (sxx_x + szx_z);
+    f[F_VZ * p.plane + i] = vzn;
+    f[F_VX * p.plane + i] = vxn;
+    if (MODE != MODE_FWD_NOWE)
+        f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i] = weo + (vxn * vxn + vzn * vzn);
+}
+
+// vsrc2 + urec2 (src/cpu/n_kernel_lib_PSV.cpp:487-576) for the sources and
+// receivers of one tile of the velocity kernel, after the tile's velocities
+// are written; then the snapshot fix-up of source cells (the stored
+// velocity is the post-injection one).  Called by every thread of the block.
+template <typename T, int MODE>
+__device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRecParams<T> &q,
+                                            int it, int slot, int tile, int bz, int tid, int nth)
+{
     if (q.src_kind < 0 && !q.rtf_z) return;  // uniform: kernel argument
-    const int tile = blockIdx.y * gridDim.x + blockIdx.x;
-    const int shot = p.ctl[0] + blockIdx.z;
-    const int tid = threadIdx.y * 32 + threadIdx.x, nth = 32 * blockDim.y;
+    const int shot = p.ctl[0] + bz;
+    T *f = p.fld + (long long)bz * p.shot_stride;
+    T *vz = f + F_VZ * p.plane;
+    T *vx = f + F_VX * p.plane;
+    const long long sp = p.snap_plane;
     int k0 = 0, k1 = 0;
     if (q.src_kind == 0) {
         const int *off = q.t_src_off + (long long)shot * (q.ntiles + 1);
@@ -371,7 +285,7 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
         }
     }
     if (slot >= 0 && q.src_kind == 0 && MODE != MODE_ADJ) {  // snapshot holds post-injection v
-        T *h = p.hist + (long long)blockIdx.z * p.hist_shot_stride + (long long)slot * p.hist_slot_stride;
+        T *h = p.hist + (long long)bz * p.hist_shot_stride + (long long)slot * p.hist_slot_stride;
         for (int k = k0 + tid; k < k1; k += nth) {
             const int j = q.t_src_k[k];
             const int c = q.src_snap[j];
@@ -381,6 +295,265 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
             h[H_VX * sp + c] = vx[pos] * p.inv_dt;
         }
     }
+}
+
+// Rows [z0, z1) x columns [x0, x1) lie inside the interior, away from the
+// CPML strips: the velocity update there is a plain stencil.
+template <typename T>
+__device__ __forceinline__ bool plain_box(const StepParams<T> &p, int z0, int z1, int x0, int x1)
+{
+    return z0 >= p.nz1 && z0 >= p.pz0 && z1 <= p.nz2 && z1 <= p.pz1 && x0 >= p.nx1 &&
+           x0 >= p.px0 && x1 <= p.nx2 && x1 <= p.px1 && p.plane < (1LL << 29);
+}
+
+// ... and for the stress update also away from every free-surface row and
+// the rows / columns it mirrors (no cell of the box is written by another
+// thread's mirror, none of its threads writes a mirror).
+template <typename T>
+__device__ __forceinline__ bool plain_stress_box(const StepParams<T> &p, int z0, int z1, int x0,
+                                                 int x1)
+{
+    bool ok = plain_box(p, z0, z1, x0, x1);
+    if (p.st) ok = ok && z0 > 2 * p.st - p.nz1;
+    if (p.sb) ok = ok && z1 - 1 < 2 * p.sb - p.nz2;
+    if (p.sl) ok = ok && x0 > 2 * p.sl - p.nx1;
+    if (p.sr) ok = ok && x1 - 1 < 2 * p.sr - p.nx2;
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Stress step, direct loads: vdiff2 + pml_diff2 + update_s2 + surf_mirror
+// (src/cpu/n_kernel_lib_PSV.cpp:100-131, 134-205, 272-395).  Interior points
+// only.
+// ---------------------------------------------------------------------------
+template <typename T, int NS, int RPT, bool SH>
+__global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
+{
+    if ((int)blockIdx.z >= p.ctl[1]) return;
+    const int ix = p.nx1 + blockIdx.x * 32 + threadIdx.x;
+    const int zb = p.nz1 + (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
+    if (zb >= p.nz2) return;  // uniform across the warp; no block barrier follows
+    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
+    {
+        const int bz0 = p.nz1 + blockIdx.y * blockDim.y * RPT, bx0 = p.nx1 + blockIdx.x * 32;
+        if (plain_stress_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32)) {
+            // no bounds, CPML or surface work: 32-bit offsets, unpredicated loads
+            const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
+            const T *__restrict__ vzc = f + F_VZ * pl + i0;
+            const T *__restrict__ vxc = f + F_VX * pl + i0;
+            T *__restrict__ szz = f + F_SZZ * pl;
+            constexpr int W = RPT + 2 * NS - 1;
+            T wz[W], wx[W];  // wz[j] = vz[zb - N + j], wx[j] = vx[zb - N + 1 + j]
+#pragma unroll
+            for (int j = 0; j < W; j++) {
+                wz[j] = vzc[(j - NS) * P];
+                wx[j] = vxc[(j - NS + 1) * P];
+            }
+#pragma unroll
+            for (int r = 0; r < RPT; r++) {
+                const T *vzr = vzc + r * P, *vxr = vxc + r * P;
+                const T oz = wz[r + NS], ox = wx[r + NS - 1];
+                T vz_z = p.cz[0] * (oz - wz[r + NS - 1]);
+                T vx_z = p.cz[0] * (wx[r + NS] - ox);
+                T vz_x = p.cx[0] * (vzr[1] - oz);
+                T vx_x = p.cx[0] * (ox - vxr[-1]);
+#pragma unroll
+                for (int k = 2; k <= NS; k++) {
+                    vz_z += p.cz[k - 1] * (wz[r + NS + k - 1] - wz[r + NS - k]);
+                    vx_z += p.cz[k - 1] * (wx[r + NS + k - 1] - wx[r + NS - k]);
+                    vz_x += p.cx[k - 1] * (vzr[k] - vzr[-(k - 1)]);
+                    vx_x += p.cx[k - 1] * (vxr[k - 1] - vxr[-k]);
+                }
+                const int i = i0 + r * P;
+                const T cl = p.c_lam[i], c2 = p.c_l2m[i], cm = p.c_muzx[i];
+                const T ozz = szz[i], ozx = szz[i + pl], oxx = szz[i + 2 * pl];
+                szz[i] = ozz + (c2 * vz_z + cl * vx_x);
+                szz[i + 2 * pl] = oxx + (cl * vz_z + c2 * vx_x);
+                szz[i + pl] = ozx + cm * (vz_x + vx_z);
+            }
+            return;
+        }
+    }
+    const long long P = p.pitch;
+    const T *__restrict__ vz = f + F_VZ * p.plane;
+    const T *__restrict__ vx = f + F_VX * p.plane;
+    T *szz = f + F_SZZ * p.plane;
+    T *szx = f + F_SZX * p.plane;
+    T *sxx = f + F_SXX * p.plane;
+    const bool colin = ix < p.nx2, colok = ix < p.nx;
+
+    // wz[j] = vz[zb - N + j], wx[j] = vx[zb - N + 1 + j]
+    constexpr int W = RPT + 2 * NS - 1;
+    T wz[W], wx[W];
+#pragma unroll
+    for (int j = 0; j < W; j++) {
+        const int rz = zb - NS + j, rx = zb - NS + 1 + j;  // >= 0: zb >= fpad >= N
+        wz[j] = (colok && rz < p.nz) ? vz[(long long)rz * P + ix] : T(0);
+        wx[j] = (colok && rx < p.nz) ? vx[(long long)rx * P + ix] : T(0);
+    }
+
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+        const int iz = zb + r;
+        const bool rowload = iz < p.nz;
+        const long long rowoff = (long long)(rowload ? iz : 0) * P;
+        const T *vzr = vz + rowoff, *vxr = vx + rowoff;
+        // staggered derivatives; term 1 is the reference's 2-point difference
+        const T oz = wz[r + NS], ox = wx[r + NS - 1];
+        T vz_z = p.cz[0] * (oz - wz[r + NS - 1]);
+        T vx_z = p.cz[0] * (wx[r + NS] - ox);
+        T vz_x = p.cx[0] * (xnb<SH>(oz, 1, vzr, ix, p.nx, rowload) - oz);
+        T vx_x = p.cx[0] * (ox - xnb<SH>(ox, -1, vxr, ix, p.nx, rowload));
+#pragma unroll
+        for (int k = 2; k <= NS; k++) {
+            vz_z += p.cz[k - 1] * (wz[r + NS + k - 1] - wz[r + NS - k]);
+            vx_z += p.cz[k - 1] * (wx[r + NS + k - 1] - wx[r + NS - k]);
+            vz_x += p.cx[k - 1] * (xnb<SH>(oz, k, vzr, ix, p.nx, rowload) -
+                                   xnb<SH>(oz, -(k - 1), vzr, ix, p.nx, rowload));
+            vx_x += p.cx[k - 1] * (xnb<SH>(ox, k - 1, vxr, ix, p.nx, rowload) -
+                                   xnb<SH>(ox, -k, vxr, ix, p.nx, rowload));
+        }
+        if (iz >= p.nz2 || !colin) continue;
+        const long long i = (long long)iz * P + ix;
+        cpml_stress(p, (int)blockIdx.z, iz, ix, vz_z, vx_z, vz_x, vx_x);
+        stress_finish(p, szz, szx, sxx, iz, ix, i, szz[i], szx[i], sxx[i], p.c_lam[i], p.c_l2m[i],
+                      p.c_muzx[i], vz_z, vx_z, vz_x, vx_x);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Velocity step, direct loads: sdiff2 + pml_diff2 + update_v2
+// (src/cpu/n_kernel_lib_PSV.cpp:207-270, 134-178), fused with the step's
+// remaining work:
+//   forward modes: gard_fwd_storage2 (:398-436) into `slot`;
+//   MODE_ADJ: u += dt v, and fwi_grad2 (:439-484, CPU sign) against `slot`;
+//   epilogue: vsrc2 + urec2 (:487-576) for the sources / receivers of the
+//   block's tile, after all of the tile's velocities are written.
+// Covers the whole grid: cells outside the interior only take part in the
+// snapshot / imaging work (their fields are never updated).
+// ---------------------------------------------------------------------------
+template <typename T, int NS, int MODE, int RPT, bool SH>
+__global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const SrcRecParams<T> q,
+                                                  const int it, const int slot)
+{
+    if ((int)blockIdx.z >= p.ctl[1]) return;  // whole block
+    const int ix = blockIdx.x * 32 + threadIdx.x;
+    const int zb = (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
+    const long long P = p.pitch;
+    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
+    const T *__restrict__ szz = f + F_SZZ * p.plane;
+    const T *__restrict__ szx = f + F_SZX * p.plane;
+    const T *__restrict__ sxx = f + F_SXX * p.plane;
+    const bool colok = ix < p.nx;
+    const bool colin = ix >= p.nx1 && ix < p.nx2;
+    const int bz0 = blockIdx.y * blockDim.y * RPT, bx0 = blockIdx.x * 32;
+    const bool plain = plain_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32);
+
+    if (plain) {  // interior, no CPML: 32-bit offsets, unpredicated loads
+        constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
+        const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
+        const T *__restrict__ zzc = f + F_SZZ * pl + i0;
+        const T *__restrict__ zxc = f + F_SZX * pl + i0;
+        const T *__restrict__ xxc = f + F_SXX * pl + i0;
+        constexpr int W = RPT + 2 * NS - 1;
+        T wzz[W], wzx[W];  // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            wzz[j] = zzc[(j - NS + 1) * P];
+            wzx[j] = zxc[(j - NS) * P];
+        }
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            const T *zxr = zxc + r * P, *xxr = xxc + r * P;
+            const T ozz = wzz[r + NS - 1], ozx = wzx[r + NS], oxx = xxr[0];
+            T szz_z = p.cz[0] * (wzz[r + NS] - ozz);
+            T szx_z = p.cz[0] * (ozx - wzx[r + NS - 1]);
+            T szx_x = p.cx[0] * (ozx - zxr[-1]);
+            T sxx_x = p.cx[0] * (xxr[1] - oxx);
+#pragma unroll
+            for (int k = 2; k <= NS; k++) {
+                szz_z += p.cz[k - 1] * (wzz[r + NS + k - 1] - wzz[r + NS - k]);
+                szx_z += p.cz[k - 1] * (wzx[r + NS + k - 1] - wzx[r + NS - k]);
+                szx_x += p.cx[k - 1] * (zxr[k - 1] - zxr[-k]);
+                sxx_x += p.cx[k - 1] * (xxr[k] - xxr[-(k - 1)]);
+            }
+            const int i = i0 + r * P;
+            const T uzo = U ? f[F_UZ * pl + i] : T(0), uxo = U ? f[F_UX * pl + i] : T(0);
+            const T weo = MODE != MODE_FWD_NOWE ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * pl + i] : T(0);
+            T vzn, vxn, uzn = T(0), uxn = T(0);
+            velocity_finish<T, MODE>(p, f, i, f[F_VZ * pl + i], f[F_VX * pl + i], uzo, uxo, weo,
+                                     p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x, sxx_x, vzn, vxn,
+                                     uzn, uxn);
+            if (slot >= 0)
+                snapshot_point<T, MODE>(p, (int)blockIdx.z, zb + r, ix, i, slot, ozz, ozx, oxx,
+                                        vzn, vxn, uzn, uxn);
+        }
+    } else if (zb < p.nz) {  // warp-uniform
+        // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
+        constexpr int W = RPT + 2 * NS - 1;
+        T wzz[W], wzx[W], wxx[RPT];
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            const int ra = zb - NS + 1 + j, rb = zb - NS + j;
+            wzz[j] = (colok && ra >= 0 && ra < p.nz) ? szz[(long long)ra * P + ix] : T(0);
+            wzx[j] = (colok && rb >= 0 && rb < p.nz) ? szx[(long long)rb * P + ix] : T(0);
+        }
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            const int iz = zb + r;
+            wxx[r] = (colok && iz < p.nz) ? sxx[(long long)iz * P + ix] : T(0);
+        }
+
+#pragma unroll
+        for (int r = 0; r < RPT; r++) {
+            const int iz = zb + r;
+            const bool rowload = iz < p.nz;
+            const long long rowoff = (long long)(rowload ? iz : 0) * P;
+            const T *szxr = szx + rowoff, *sxxr = sxx + rowoff;
+            const T ozz = wzz[r + NS - 1], ozx = wzx[r + NS], oxx = wxx[r];
+            T szz_z = p.cz[0] * (wzz[r + NS] - ozz);
+            T szx_z = p.cz[0] * (ozx - wzx[r + NS - 1]);
+            T szx_x = p.cx[0] * (ozx - xnb<SH>(ozx, -1, szxr, ix, p.nx, rowload));
+            T sxx_x = p.cx[0] * (xnb<SH>(oxx, 1, sxxr, ix, p.nx, rowload) - oxx);
+#pragma unroll
+            for (int k = 2; k <= NS; k++) {
+                szz_z += p.cz[k - 1] * (wzz[r + NS + k - 1] - wzz[r + NS - k]);
+                szx_z += p.cz[k - 1] * (wzx[r + NS + k - 1] - wzx[r + NS - k]);
+                szx_x += p.cx[k - 1] * (xnb<SH>(ozx, k - 1, szxr, ix, p.nx, rowload) -
+                                        xnb<SH>(ozx, -k, szxr, ix, p.nx, rowload));
+                sxx_x += p.cx[k - 1] * (xnb<SH>(oxx, k, sxxr, ix, p.nx, rowload) -
+                                        xnb<SH>(oxx, -(k - 1), sxxr, ix, p.nx, rowload));
+            }
+            if (!rowload || !colok) continue;
+            const long long i = (long long)iz * P + ix;
+            const bool inner = colin && iz >= p.nz1 && iz < p.nz2;
+            T vzn, vxn, uzn = T(0), uxn = T(0);
+            if (inner) {
+                cpml_velocity(p, (int)blockIdx.z, iz, ix, szz_z, szx_z, szx_x, sxx_x);
+                constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
+                const T uzo = U ? f[F_UZ * p.plane + i] : T(0);
+                const T uxo = U ? f[F_UX * p.plane + i] : T(0);
+                const T weo = MODE != MODE_FWD_NOWE
+                                  ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i]
+                                  : T(0);
+                velocity_finish<T, MODE>(p, f, i, f[F_VZ * p.plane + i], f[F_VX * p.plane + i],
+                                         uzo, uxo, weo, p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x,
+                                         sxx_x, vzn, vxn, uzn, uxn);
+            } else {
+                vzn = f[F_VZ * p.plane + i];
+                vxn = f[F_VX * p.plane + i];
+                if (MODE == MODE_ADJ || MODE == MODE_FWD_U) {
+                    uzn = f[F_UZ * p.plane + i];
+                    uxn = f[F_UX * p.plane + i];
+                }
+            }
+            if (slot >= 0)
+                snapshot_point<T, MODE>(p, (int)blockIdx.z, iz, ix, i, slot, ozz, ozx, oxx, vzn,
+                                        vxn, uzn, uxn);
+        }
+    }
+    srcrec_tile<T, MODE>(p, q, it, slot, blockIdx.y * gridDim.x + blockIdx.x, (int)blockIdx.z,
+                         threadIdx.y * 32 + threadIdx.x, 32 * blockDim.y);
 }
 
 // ---------------------------------------------------------------------------

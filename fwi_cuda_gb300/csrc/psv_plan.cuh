@@ -1,6 +1,7 @@
 // psv_plan.cuh -- the device-resident survey plan (host C++ side).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <memory>
@@ -24,6 +25,22 @@ cudaError_t launch_zero_planes(T *base, long long shot_stride, long long off, lo
                                int nbatch, cudaStream_t st);
 cudaError_t launch_transpose(const double *in, double *out, int rows, int cols, int nbatch,
                              cudaStream_t st);
+
+// TMA tile kernels (FP32, psv_tiled.cu): tiles of 64 columns x 4 rpt rows,
+// rpt in {2, 4, 8}.  Maps of one field block: halo'd and own boxes of the
+// field planes, own boxes of the 7 coefficient planes.
+struct TileMaps {
+    CUtensorMap halo;  // field planes, box 72 x (4 rpt + 2 ns)
+    CUtensorMap own;   // field planes, box 64 x 4 rpt
+    CUtensorMap coef;  // coefficient planes, box 64 x 4 rpt
+};
+int encode_tile_maps(TileMaps *m, const float *fld, int nfplanes, const float *coef, int nx, int nz,
+                     int pitch, long long plane, int ns, int rpt);
+cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
+                              int nbatch, cudaStream_t st);
+cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,
+                                const TileMaps &m, int ns, int mode, int it, int slot, int rpt,
+                                int nbatch, cudaStream_t st);
 
 #define PSV_CU(call)                                                                        \
     do {                                                                                    \
@@ -109,7 +126,8 @@ struct PlanIface {
     virtual void *stream() const = 0;
     virtual long long launches() const = 0;
     virtual int profile(int nsteps, double *ms6) = 0;
-    virtual int autotune(int nsteps, int *rpt, int *by) = 0;
+    virtual int autotune(int nsteps, int *fam, int *rpt, int *by) = 0;
+    virtual void shape(int *fam, int *rpt, int *by) const = 0;
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
                             const double *rho_zp, const double *rho_xp, int ishot, int grad,

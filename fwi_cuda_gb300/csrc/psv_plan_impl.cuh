@@ -15,11 +15,11 @@ namespace psv {
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
 
 // Process-wide cache of autotuned tile shapes: (nz, nx, stencil terms, batch,
-// element size, interior rows) -> (rows per thread, block height).
+// element size, requested family) -> (family, rows per thread, block height).
 using TuneKey = std::tuple<int, int, int, int, int, int>;
-inline std::map<TuneKey, std::pair<int, int>> &tune_cache()
+inline std::map<TuneKey, std::tuple<int, int, int>> &tune_cache()
 {
-    static std::map<TuneKey, std::pair<int, int>> m;
+    static std::map<TuneKey, std::tuple<int, int, int>> m;
     return m;
 }
 inline std::mutex &tune_mutex()
@@ -56,6 +56,9 @@ public:
     DevMem f_off, f_pos, f_col, f_snap, a_off, a_pos, a_col, a_snap, rec_pos;
     DevMem t_src_off, t_src_k, t_rec_off, t_rec_r;  // per-tile source / receiver index
     int rpt = 1;                                     // rows per thread (< 0: shuffle variant)
+    int fam = PSV_KERNELS_DIRECT;                    // kernel family of the time step
+    TileMaps tmap{}, tmap2{};                        // tensor maps of fld / fld2 (TMA family)
+    int *h_err = nullptr;                            // pinned copy of the device error word
     std::vector<int> h_f_off;                        // host copy of the per-shot source lists
     // Checkpointed storage: state checkpoints every K steps, a recompute
     // state (5 field planes + CPML strips) and a segment snapshot buffer.
@@ -85,6 +88,7 @@ public:
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
         if (h_ctl) cudaFreeHost(h_ctl);
+        if (h_err) cudaFreeHost(h_err);
         if (st) cudaStreamDestroy(st);
     }
 
@@ -122,9 +126,19 @@ public:
         const psv_grid &g = sv.g;
         const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
         const int al = 128 / (int)sizeof(T);
+        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_TMA)
+            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1 or 2");
+        if (opt.kernel_family == PSV_KERNELS_TMA && sizeof(T) != 4)
+            return fail(PSV_ERR_UNSUPPORTED, "TMA tile kernels are FP32 only");
         if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
         if (opt.block_y > 0 || opt.rows_per_thread) opt.autotune = 0;  // explicit shape wins
-        rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
+        if (opt.kernel_family == PSV_KERNELS_TMA) {
+            fam = PSV_KERNELS_TMA;
+            rpt = tma_rpt(opt.rows_per_thread ? opt.rows_per_thread : 4);
+        } else {
+            rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
+            if (opt.block_y <= 0) blk = dim3(32, 4, 1);
+        }
         pitch = round_up(nx, al);
         plane = (long long)nz * pitch;
         shot_stride = NFIELD * plane;
@@ -176,6 +190,8 @@ public:
         PSV_CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         for (auto &e : ev) PSV_CU(cudaEventCreate(&e));
         PSV_CU(cudaMallocHost(&h_ctl, sizeof(int) * 2 * nbatch));
+        PSV_CU(cudaMallocHost(&h_err, sizeof(int)));
+        *h_err = 0;
         for (int b = 0; b < nbatch; b++) {
             h_ctl[2 * b] = b * B;
             h_ctl[2 * b + 1] = std::min(B, nshot - b * B);
@@ -193,7 +209,8 @@ public:
         PSV_TRY(traces.alloc((size_t)6 * nshot * ntr * 8 + 8, total));
         PSV_TRY(red.alloc(((size_t)256 * std::max(3, nshot) + nshot + 3 + B + 2) * 8, total));
         PSV_TRY(taperb.alloc((size_t)(nx + nz) * 8, total));
-        PSV_TRY(ctl.alloc(2 * sizeof(int), total));
+        PSV_TRY(ctl.alloc(4 * sizeof(int), total));
+        PSV_CU(cudaMemsetAsync(ctl.p, 0, 4 * sizeof(int), st));
         PSV_TRY(scales.alloc((size_t)4 * nshot * 8, total));
         {
             std::vector<double> one((size_t)3 * nshot, 1.0);
@@ -210,7 +227,62 @@ public:
         PSV_TRY(upload_sources());
         PSV_TRY(upload_taper());
         fill_params();
+        PSV_TRY(encode_maps());
         PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    static int tma_rpt(int r) { return (r == 2 || r == 4 || r == 8) ? r : 4; }
+
+    // Tensor maps of the field blocks for the TMA family (rebuilt when the
+    // tile height or a field buffer changes).
+    int encode_maps()
+    {
+        if constexpr (sizeof(T) == 4) {
+            if (fam != PSV_KERNELS_TMA) return PSV_OK;
+            const psv_grid &g = sv.g;
+            PSV_TRY(encode_tile_maps(&tmap, fld.as<float>(), (int)(B * NFIELD), coef.as<float>(),
+                                     g.nx, g.nz, pitch, plane, sv.ns, rpt));
+            if (fld2.p)
+                PSV_TRY(encode_tile_maps(&tmap2, fld2.as<float>(), B * 5, coef.as<float>(), g.nx,
+                                         g.nz, pitch, plane, sv.ns, rpt));
+        }
+        return PSV_OK;
+    }
+
+    // One stress / velocity launch of the current kernel family; `second`
+    // selects the checkpoint recompute state.
+    cudaError_t ks(const StepParams<T> &s, bool second)
+    {
+        if constexpr (sizeof(T) == 4)
+            if (fam == PSV_KERNELS_TMA)
+                return launch_stress_tma(s, second ? tmap2 : tmap, sv.ns, rpt, B, st);
+        (void)second;
+        return launch_stress<T>(s, sv.ns, rpt, blk, B, st);
+    }
+    cudaError_t kv(const StepParams<T> &s, const SrcRecParams<T> &q, int mode, int it, int slot,
+                   bool second)
+    {
+        if constexpr (sizeof(T) == 4)
+            if (fam == PSV_KERNELS_TMA)
+                return launch_velocity_tma(s, q, second ? tmap2 : tmap, sv.ns, mode, it, slot, rpt,
+                                           B, st);
+        (void)second;
+        return launch_velocity<T>(s, q, sv.ns, mode, it, slot, rpt, blk, B, st);
+    }
+
+    // Wait for the stream, then fail if a time-step kernel gave up a bounded
+    // wait (device error word).
+    int sync_check()
+    {
+        PSV_CU(cudaMemcpyAsync(h_err, ctl.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        if (*h_err) {
+            *h_err = 0;
+            PSV_CU(cudaMemsetAsync(ctl.as<int>() + 2, 0, sizeof(int), st));
+            PSV_CU(cudaStreamSynchronize(st));
+            return fail(PSV_ERR_CUDA, "time-step kernel: a tile copy did not complete in time");
+        }
         return PSV_OK;
     }
 
@@ -287,14 +359,18 @@ public:
         return PSV_OK;
     }
 
-    // Sources and receivers bucketed by the velocity kernel's tiles (32
-    // columns x blk.y * rpt rows), so each block finds its own.
+    // Sources and receivers bucketed by the velocity kernel's tiles (direct
+    // family: 32 columns x blk.y * |rpt| rows; TMA family: 64 x 4 rpt), so
+    // each block finds its own.
     int build_tile_index()
     {
         const int nshot = sv.s.nshot, nrec = sv.s.nrec;
-        const int tz = (int)blk.y * (rpt < 0 ? -rpt : rpt), ntx = (sv.g.nx + 31) / 32, ntz = (sv.g.nz + tz - 1) / tz;
+        const bool tma = fam == PSV_KERNELS_TMA;
+        const int tw = tma ? 64 : 32;
+        const int tz = tma ? 4 * rpt : (int)blk.y * (rpt < 0 ? -rpt : rpt);
+        const int ntx = (sv.g.nx + tw - 1) / tw, ntz = (sv.g.nz + tz - 1) / tz;
         const int nt_ = ntx * ntz;
-        auto tile_of = [&](int z, int x) { return (z / tz) * ntx + x / 32; };
+        auto tile_of = [&](int z, int x) { return (z / tz) * ntx + x / tw; };
         std::vector<int> soff((size_t)nshot * (nt_ + 1), 0), sk;
         std::vector<std::vector<int>> b(nt_);
         for (int s_ = 0; s_ < nshot; s_++) {
@@ -421,6 +497,7 @@ public:
         p.gshot = gshot.as<T>();
         p.gshot_shot_stride = gshot_shot;
         p.ctl = ctl.as<int>();
+        p.err = ctl.as<int>() + 2;
 
         SrcRecParams<T> q{};
         q.src_off = f_off.as<int>(); q.src_pos = f_pos.as<int>(); q.src_col = f_col.as<int>();
@@ -470,6 +547,7 @@ public:
             sp2.memx = memx2.as<T>();
         }
         sp2.hist = hist.as<T>();
+        PSV_TRY(encode_maps());
         drop_graphs();
         return PSV_OK;
     }
@@ -540,8 +618,8 @@ public:
             // forward keeping a state checkpoint at the start of every K-step segment
             for (int it = 0; it < nt; it++) {
                 if (!(it % K)) PSV_TRY(ck_copy(it / K, true));
-                PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
-                PSV_CU(launch_velocity<T>(sp, qf, sv.ns, mode, it, -1, rpt, blk, B, st));
+                PSV_CU(ks(sp, false));
+                PSV_CU(kv(sp, qf, mode, it, -1, false));
             }
             nk += 2LL * nt;
         } else if (ckpt && kind == PASS_ADJ_RES) {
@@ -553,13 +631,13 @@ public:
                 PSV_TRY(ck_copy(j, false));
                 for (int it = a; it < e; it++) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(launch_stress<T>(sp2, sv.ns, rpt, blk, B, st));
-                    PSV_CU(launch_velocity<T>(sp2, qr, sv.ns, MODE_FWD_NOWE, it, slot, rpt, blk, B, st));
+                    PSV_CU(ks(sp2, true));
+                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, slot, true));
                 }
                 for (int it = e - 1; it >= a; it--) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
-                    PSV_CU(launch_velocity<T>(sp, qa, sv.ns, MODE_ADJ, it, slot, rpt, blk, B, st));
+                    PSV_CU(ks(sp, false));
+                    PSV_CU(kv(sp, qa, MODE_ADJ, it, slot, false));
                 }
             }
             nk += 4LL * nt;
@@ -567,9 +645,8 @@ public:
             for (int jt = 0; jt < nt; jt++) {
                 const int it = adj ? nt - 1 - jt : jt;
                 const bool snap = !(it % sdt);
-                PSV_CU(launch_stress<T>(sp, sv.ns, rpt, blk, B, st));
-                PSV_CU(launch_velocity<T>(sp, q, sv.ns, mode, it,
-                                          (snap && (store || adj)) ? it / sdt : -1, rpt, blk, B, st));
+                PSV_CU(ks(sp, false));
+                PSV_CU(kv(sp, q, mode, it, (snap && (store || adj)) ? it / sdt : -1, false));
             }
             nk += 2LL * nt;
         }
@@ -727,7 +804,7 @@ public:
         PSV_CU(cudaEventRecord(ev[1], st));
         if (uz && sv.s.nrec) PSV_TRY(download_traces(uz, tr(0), 0, sv.s.nshot));
         if (ux && sv.s.nrec) PSV_TRY(download_traces(ux, tr(1), 0, sv.s.nshot));
-        PSV_CU(cudaStreamSynchronize(st));
+        PSV_TRY(sync_check());
         float ms = 0;
         PSV_CU(cudaEventElapsedTime(&ms, ev[0], ev[1]));
         t_ms[0] = ms; t_ms[1] = 0; t_ms[2] = 0;
@@ -760,7 +837,7 @@ public:
             PSV_TRY(run_pass(PASS_ADJ_RES));
             PSV_CU(cudaEventRecord(ev[3], st));
             PSV_TRY(precondition(n));
-            PSV_CU(cudaStreamSynchronize(st));
+            PSV_TRY(sync_check());
             float a, c, d;
             PSV_CU(cudaEventElapsedTime(&a, ev[0], ev[1]));
             PSV_CU(cudaEventElapsedTime(&c, ev[1], ev[2]));
@@ -891,7 +968,7 @@ public:
         }
         std::vector<double> h(sv.s.nshot);
         PSV_CU(cudaMemcpyAsync(h.data(), L2dev(), h.size() * 8, cudaMemcpyDeviceToHost, st));
-        PSV_CU(cudaStreamSynchronize(st));
+        PSV_TRY(sync_check());
         double s = 0.0;
         for (double v : h) s += v;
         *L2 = s;
@@ -968,10 +1045,13 @@ public:
 
     // Switch the stencil kernels' tile shape (rebuilds the per-tile source
     // index, drops captured graphs).
-    int set_shape(int r, int by)
+    int set_shape(int f, int r, int by)
     {
-        r = rpt_ok<T>(r);
-        if (r == rpt && (int)blk.y == by) return PSV_OK;
+        if (f == PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
+        r = f == PSV_KERNELS_TMA ? tma_rpt(r) : rpt_ok<T>(r);
+        if (f == PSV_KERNELS_TMA) by = 4;
+        if (f == fam && r == rpt && (int)blk.y == by) return PSV_OK;
+        fam = f;
         rpt = r;
         blk = dim3(32, by, 1);
         PSV_TRY(build_tile_index());
@@ -980,53 +1060,71 @@ public:
         qf.t_rec_off = qr.t_rec_off = qk.t_rec_off = qa.t_rec_off = t_rec_off.as<int>();
         qf.t_rec_r = qr.t_rec_r = qk.t_rec_r = qa.t_rec_r = t_rec_r.as<int>();
         qf.ntiles = qr.ntiles = qk.ntiles = qa.ntiles = ntiles;
+        PSV_TRY(encode_maps());
         drop_graphs();
         return PSV_OK;
     }
 
-    int autotune(int nsteps, int *out_rpt, int *out_by) override
+    int autotune(int nsteps, int *out_fam, int *out_rpt, int *out_by) override
     {
-        const TuneKey key{sv.g.nz, sv.g.nx, sv.ns, B, (int)sizeof(T), sv.nz2 - sv.nz1};
+        const TuneKey key{sv.g.nz, sv.g.nx, sv.ns, B, (int)sizeof(T), opt.kernel_family};
+        auto report = [&] {
+            if (out_fam) *out_fam = fam;
+            if (out_rpt) *out_rpt = rpt;
+            if (out_by) *out_by = (int)blk.y;
+        };
         {
             std::lock_guard<std::mutex> lk(tune_mutex());
             auto it = tune_cache().find(key);
             if (it != tune_cache().end()) {
-                PSV_TRY(set_shape(it->second.first, it->second.second));
+                PSV_TRY(set_shape(std::get<0>(it->second), std::get<1>(it->second),
+                                  std::get<2>(it->second)));
                 tuned = true;
-                if (out_rpt) *out_rpt = rpt;
-                if (out_by) *out_by = (int)blk.y;
+                report();
                 return PSV_OK;
             }
         }
-        static const int rpts32[] = {1, 2, 4, -2, -4}, rpts64[] = {1};
-        static const int bys[] = {2, 4, 8};
-        const int *rp = sizeof(T) == 8 ? rpts64 : rpts32;
-        const int nr = sizeof(T) == 8 ? 1 : 5;
-        double best = 1e30;
-        int br = rpt, bb = (int)blk.y;
-        for (int i = 0; i < nr; i++)
-            for (int by : bys) {
-                PSV_TRY(set_shape(rp[i], by));
-                double ms[6];
-                PSV_TRY(profile(nsteps, ms));
-                const double t = ms[0] + ms[1] + ms[3] + ms[4];
-                if (t < best) { best = t; br = rpt; bb = by; }
+        // candidates: direct loads (rows per thread x block height), TMA tiles (rows per thread)
+        std::vector<std::tuple<int, int, int>> cand;
+        if (opt.kernel_family != PSV_KERNELS_TMA) {
+            const int r32[] = {1, 2, 4, -2, -4};
+            for (int r : r32) {
+                if (sizeof(T) == 8 && r != 1) continue;
+                for (int by : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_DIRECT, r, by);
             }
-        PSV_TRY(set_shape(br, bb));
+        }
+        if (sizeof(T) == 4 && opt.kernel_family != PSV_KERNELS_DIRECT)
+            for (int r : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_TMA, r, 4);
+        double best = 1e30;
+        std::tuple<int, int, int> pick{fam, rpt, (int)blk.y};
+        for (auto &c : cand) {
+            PSV_TRY(set_shape(std::get<0>(c), std::get<1>(c), std::get<2>(c)));
+            double ms[6];
+            PSV_TRY(profile(nsteps, ms));
+            const double t = ms[0] + ms[1] + ms[3] + ms[4];
+            if (t < best) { best = t; pick = {fam, rpt, (int)blk.y}; }
+        }
+        PSV_TRY(set_shape(std::get<0>(pick), std::get<1>(pick), std::get<2>(pick)));
         {
             std::lock_guard<std::mutex> lk(tune_mutex());
-            tune_cache()[key] = {br, bb};
+            tune_cache()[key] = pick;
         }
         tuned = true;
-        if (out_rpt) *out_rpt = br;
-        if (out_by) *out_by = bb;
+        report();
         return PSV_OK;
+    }
+
+    void shape(int *f, int *r, int *by) const override
+    {
+        if (f) *f = fam;
+        if (r) *r = rpt;
+        if (by) *by = fam == PSV_KERNELS_TMA ? 4 : (int)blk.y;
     }
 
     int maybe_autotune()
     {
         if (tuned || !opt.autotune || !have_model || !have_obs) return PSV_OK;
-        return autotune(std::min(24, sv.g.nt), nullptr, nullptr);
+        return autotune(std::min(24, sv.g.nt), nullptr, nullptr, nullptr);
     }
 
     void *stream() const override { return (void *)st; }
@@ -1056,20 +1154,17 @@ public:
                 const int slot = !(it % sdt) ? (it / sdt) % (ckpt ? nslots : sv.snt) : -1;
                 cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
                 cudaEventRecord(E[0], st);
-                cudaError_t c = launch_stress<T>(sp, sv.ns, rpt, blk, B, st);
+                cudaError_t c = ks(sp, false);
                 cudaEventRecord(E[1], st);
                 if (c == cudaSuccess)
-                    c = launch_velocity<T>(sp, q, sv.ns, adj ? MODE_ADJ : MODE_FWD, it, slot, rpt, blk, B, st);
+                    c = kv(sp, q, adj ? MODE_ADJ : MODE_FWD, it, slot, false);
                 cudaEventRecord(E[2], st);
                 cudaEventRecord(E[3], st);
                 if (c != cudaSuccess) { rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c)); break; }
                 nlaunch += 2;
             }
         }
-        if (rc == PSV_OK) {
-            cudaError_t c = cudaStreamSynchronize(st);
-            if (c != cudaSuccess) rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c));
-        }
+        if (rc == PSV_OK) rc = sync_check();
         for (int k = 0; k < 6; k++) ms6[k] = 0.0;
         if (rc == PSV_OK)
             for (int pass = 0; pass < 2; pass++)
@@ -1132,7 +1227,7 @@ public:
             PSV_TRY(run_pass(PASS_FWD_U));
             store_flag = false;
         }
-        PSV_CU(cudaStreamSynchronize(st));
+        PSV_TRY(sync_check());
         // wavefields: vz vx uz ux szz szx sxx We
         std::vector<T> pl((size_t)shot_stride);
         PSV_CU(cudaMemcpy(pl.data(), fld.p, pl.size() * sizeof(T), cudaMemcpyDeviceToHost));

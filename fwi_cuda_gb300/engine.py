@@ -21,7 +21,8 @@ from ._lib import PsvOptions, check, dptr, f64, i32, iptr
 
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
-            block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True) -> PsvOptions:
+            block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
+            kernels="any") -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -33,6 +34,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.checkpoint_interval = int(checkpoint_interval)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
+    o.kernel_family = {"any": 0, "direct": 1, "tma": 2}[kernels]
     return o
 
 
@@ -161,9 +163,18 @@ class Plan:
         return int(_lib.lib().psv_plan_kernel_launches(self.h))
 
     def autotune(self, nsteps=24):
-        r, b = C.c_int(), C.c_int()
-        check(_lib.lib().psv_plan_autotune(self.h, int(nsteps), C.byref(r), C.byref(b)))
-        return r.value, b.value
+        """Pick the fastest time-step kernels; returns (family, rows_per_thread,
+        block_y) with family "direct" or "tma"."""
+        f, r, b = C.c_int(), C.c_int(), C.c_int()
+        check(_lib.lib().psv_plan_autotune(self.h, int(nsteps), C.byref(f), C.byref(r), C.byref(b)))
+        return {1: "direct", 2: "tma"}[f.value], r.value, b.value
+
+    @property
+    def shape(self):
+        """(family, rows_per_thread, block_y) of the kernels the plan launches now."""
+        f, r, b = C.c_int(), C.c_int(), C.c_int()
+        check(_lib.lib().psv_plan_shape(self.h, C.byref(f), C.byref(r), C.byref(b)))
+        return {1: "direct", 2: "tma"}[f.value], r.value, b.value
 
     def profile_kernels(self, nsteps=100):
         ms = np.zeros(6)

@@ -47,6 +47,10 @@ typedef enum {
 #define PSV_STORE_FULL 1        /* every snapshot kept in HBM (the reference's accu_*) */
 #define PSV_STORE_CHECKPOINT 2  /* checkpoints + recomputation of the forward */
 
+/* Time-step kernel families (psv_options.kernel_family). */
+#define PSV_KERNELS_DIRECT 1    /* per-thread loads of the stencil neighbours */
+#define PSV_KERNELS_TMA 2       /* tiles staged in shared memory by TMA tensor copies (FP32) */
+
 const char *psv_error_string(int status);
 /* Message of the last failing call on this host thread. */
 const char *psv_last_error(void);
@@ -123,8 +127,10 @@ typedef struct psv_options {
     int max_batch;              /* shots per launch; 0 = all shots of the survey */
     int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
     int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
-    int rows_per_thread;        /* rows each thread marches: 1, 2, 4 (negative: warp-shuffle
-                                   variant); 0 = default */
+    int rows_per_thread;        /* rows each thread marches: direct family 1, 2, 4 (negative:
+                                   warp-shuffle variant); TMA family 2, 4, 8; 0 = default */
+    int kernel_family;          /* time-step kernels: 0 = any (the autotuner chooses),
+                                   PSV_KERNELS_DIRECT, PSV_KERNELS_TMA (FP32 only) */
     int autotune;               /* 1 (default): time the tile-shape candidates on the first
                                    time loop and keep the fastest (psv_plan_autotune);
                                    0: use block_y / rows_per_thread as given */
@@ -259,13 +265,18 @@ int psv_update_model(psv_plan *plan, double step);
  * everything else. */
 int psv_last_timing(const psv_plan *plan, double *ms3);
 
-/* Tile-shape autotuner: times every (rows per thread, block height)
- * candidate of the stencil kernels over nsteps forward + nsteps adjoint
- * steps (CUDA events) and keeps the fastest.  Results are cached per
- * (grid, stencil order, batch, precision) for the process.  Needs a model
- * and observed traces (it runs the kernels on them); leaves the wavefields
- * undefined.  Outputs the chosen shape. */
-int psv_plan_autotune(psv_plan *plan, int nsteps, int *rows_per_thread, int *block_y);
+/* Time-step kernel autotuner: times every candidate (kernel family, rows
+ * per thread, block height) over nsteps forward + nsteps adjoint steps
+ * (CUDA events) and keeps the fastest.  Results are cached per (grid,
+ * stencil order, batch, precision, requested family) for the process.
+ * Needs a model and observed traces (it runs the kernels on them); leaves
+ * the wavefields undefined.  Outputs the chosen shape (any pointer may be
+ * NULL). */
+int psv_plan_autotune(psv_plan *plan, int nsteps, int *kernel_family, int *rows_per_thread,
+                      int *block_y);
+/* The time-step kernels the plan launches now: family (PSV_KERNELS_*), rows
+ * per thread and block height (any pointer may be NULL). */
+int psv_plan_shape(const psv_plan *plan, int *kernel_family, int *rows_per_thread, int *block_y);
 
 /* The CUDA stream every call of this plan runs on (a cudaStream_t), for
  * callers that time or order work against it. */

@@ -1,5 +1,5 @@
-"""Tile-shape autotuner: every candidate shape computes the same gradient,
-and the tuned plan matches the oracle like any other."""
+"""Time-step kernel families and shapes: every candidate the autotuner may
+pick computes the same gradient, and the tuned plan matches the oracle."""
 import numpy as np
 import pytest
 
@@ -14,7 +14,9 @@ def _grad(sv, init, uz, ux, **opt):
         p.set_model(*init)
         p.set_observed(uz, ux)
         L2, g = p.gradient()
-        return L2, g, p
+        fam, rpt, _ = p.shape
+        assert fam == opt["kernels"] and rpt == opt["rows_per_thread"]  # the shape asked for ran
+        return L2, g
 
 
 def test_autotune_shape_and_parity(gpu, orc):
@@ -24,22 +26,71 @@ def test_autotune_shape_and_parity(gpu, orc):
     with engine.Plan(sv, precision=32) as p:
         p.set_model(*init)
         p.set_observed(uz, ux)
-        rpt, by = p.autotune(8)
-        assert rpt in (1, 2, 4, -2, -4) and by in (2, 4, 8)
+        fam, rpt, by = p.autotune(8)
+        assert (fam == "direct" and rpt in (1, 2, 4, -2, -4) and by in (2, 4, 8)) or \
+               (fam == "tma" and rpt in (2, 4, 8))
+        assert p.shape == (fam, rpt, by)
         L2, g = p.gradient()
     assert L2 == pytest.approx(L2_ref, rel=1e-4)
     for a, b in zip(g, g_ref):
         assert helpers.rel_l2(a, b) < 1e-4
 
 
-@pytest.mark.parametrize("rpt,by", [(2, 4), (4, 2), (-2, 4), (-4, 8)])
-def test_every_shape_gives_the_same_gradient(gpu, orc, rpt, by):
-    # register blocking and warp shuffles change which thread loads a value,
-    # not the arithmetic on it: results agree to rounding of the FP32 sums
-    sv, true, init = helpers.case(fdorder=8, stencil="holberg", nshot=2, nt=200, nz=75, nx=97)
+SHAPES = [("direct", 2, 4), ("direct", 4, 2), ("direct", -2, 4), ("direct", -4, 8),
+          ("tma", 2, 0), ("tma", 4, 0), ("tma", 8, 0)]
+
+
+@pytest.mark.parametrize("fam,rpt,by", SHAPES)
+@pytest.mark.parametrize("fdorder", [4, 8])
+def test_every_shape_gives_the_same_gradient(gpu, orc, fam, rpt, by, fdorder):
+    # register blocking, warp shuffles and shared-memory staging change which
+    # thread loads a value and how the compiler contracts multiply-adds, not
+    # the operations: shapes agree to FP32 rounding (1e-5, ten times tighter
+    # than the bar against the FP64 oracle)
+    sv, true, init = helpers.case(fdorder=fdorder, stencil="holberg", nshot=2, nt=200, nz=75,
+                                  nx=97)
     uz, ux = orc.simulate_fwd(sv, *true)
-    L2a, ga, _ = _grad(sv, init, uz, ux, rows_per_thread=1, block=(32, 8))
-    L2b, gb, _ = _grad(sv, init, uz, ux, rows_per_thread=rpt, block=(32, by))
+    L2a, ga = _grad(sv, init, uz, ux, kernels="direct", rows_per_thread=1, block=(32, 8))
+    L2b, gb = _grad(sv, init, uz, ux, kernels=fam, rows_per_thread=rpt, block=(32, by))
     assert L2b == pytest.approx(L2a, rel=1e-6)
     for a, b in zip(ga, gb):
-        assert helpers.rel_l2(b, a) < 1e-6
+        assert helpers.rel_l2(b, a) < 1e-5
+
+
+@pytest.mark.parametrize("kw", [dict(fdorder=2, stencil="reference", nshot=3, nt=300),
+                                dict(fdorder=6, stencil="holberg", nshot=2, nt=250,
+                                     imaging_sign=1),
+                                dict(fdorder=4, stencil="holberg", nshot=1, nt=250,
+                                     surf_offset=3)])
+def test_tma_family_against_oracle(gpu, orc, kw):
+    sv, true, init = helpers.case(nz=70, nx=130, **kw)
+    uz_ref, ux_ref = orc.simulate_fwd(sv, *true)
+    L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz_ref, ux_ref)
+    with engine.Plan(sv, precision=32, kernels="tma", rows_per_thread=4) as p:
+        assert p.shape == ("tma", 4, 4)
+        p.set_model(*true)
+        uz, ux = p.forward()
+        assert helpers.rel_l2(uz, uz_ref) < 1e-5 and helpers.rel_l2(ux, ux_ref) < 1e-5
+        p.set_model(*init)
+        p.set_observed(uz_ref, ux_ref)
+        L2, g = p.gradient()
+    assert L2 == pytest.approx(L2_ref, rel=1e-4)
+    for a, b in zip(g, g_ref):
+        assert helpers.rel_l2(a, b) < 1e-4
+
+
+def test_tma_family_checkpointed_equals_full(gpu, orc):
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, snap_dt=3)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    out = []
+    for storage in ("full", "checkpoint"):
+        with engine.Plan(sv, precision=32, kernels="tma", rows_per_thread=2,
+                         storage=storage, checkpoint_interval=40) as p:
+            assert p.shape[0] == "tma"
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            out.append(p.gradient())
+    (La, ga), (Lb, gb) = out
+    assert La == Lb
+    for a, b in zip(ga, gb):
+        assert np.array_equal(a, b)

@@ -119,3 +119,36 @@ def test_plan_validation_errors():
     assert _create(sv, precision=16) == _lib.PSV_ERR_ARG
     if not _lib.device_available():
         assert _create(sv) == _lib.PSV_ERR_CUDA  # valid survey, no device: no CPU fallback
+
+
+def _header_struct_fields(name):
+    """Field names of `typedef struct name {...} name;` in declaration order."""
+    text = open(helpers.__file__.replace("tests/helpers.py", "include/fwi_psv.h")).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), text, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        # "int a, b" / "double hc[7]" / "const double *a_z, *b_z"
+        first, *rest = decl.split(",")
+        names.append(re.findall(r"(\w+)\s*(?:\[\d+\])?\s*$", first)[0])
+        names += [re.findall(r"(\w+)\s*(?:\[\d+\])?\s*$", r)[0] for r in rest]
+    return names
+
+
+@pytest.mark.parametrize("cname,pyclass", [("psv_grid", _lib.PsvGrid), ("psv_shots", _lib.PsvShots),
+                                           ("psv_options", _lib.PsvOptions)])
+def test_ctypes_structs_match_the_header(cname, pyclass):
+    # a field out of order silently hands the library the wrong option
+    assert [f[0] for f in pyclass._fields_] == _header_struct_fields(cname)
+
+
+def test_options_reach_the_library_in_order():
+    o = engine.options(precision=32, kernels="tma", autotune=False, rows_per_thread=8)
+    raw = C.string_at(C.addressof(o), C.sizeof(o))
+    fields = dict(_lib.PsvOptions._fields_)
+    off = {n: getattr(_lib.PsvOptions, n).offset for n in fields}
+    as_int = lambda n: int.from_bytes(raw[off[n]:off[n] + 4], "little", signed=True)
+    assert as_int("kernel_family") == 2 and as_int("autotune") == 0 and as_int("rows_per_thread") == 8
