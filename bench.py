@@ -347,7 +347,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--kernels", choices=["auto", "direct", "tma"], default="auto",
+    ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4"], default="auto",
                     help="time-step kernel family (auto: the plan's autotuner picks)")
     ap.add_argument("--rpt", type=int, default=0, help="rows per thread with --kernels")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])

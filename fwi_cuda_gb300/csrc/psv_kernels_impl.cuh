@@ -321,6 +321,74 @@ __device__ __forceinline__ bool plain_stress_box(const StepParams<T> &p, int z0,
     return ok;
 }
 
+// Value of field plane `a` at (iz, ix), zero outside the grid (the values the
+// reference's padded arrays hold there).
+template <typename T>
+__device__ __forceinline__ T at(const StepParams<T> &p, const T *a, int iz, int ix)
+{
+    return (iz >= 0 && iz < p.nz && ix >= 0 && ix < p.nx) ? a[(long long)iz * p.pitch + ix] : T(0);
+}
+
+// Whole stress update of interior point (iz, ix) of batch shot bz with
+// checked loads, the same operations as the kernels' unrolled windows.
+template <typename T, int NS>
+__device__ __forceinline__ void stress_point(const StepParams<T> &p, int bz, int iz, int ix)
+{
+    T *f = p.fld + (long long)bz * p.shot_stride;
+    const T *vz = f + F_VZ * p.plane, *vx = f + F_VX * p.plane;
+    const T oz = at(p, vz, iz, ix), ox = at(p, vx, iz, ix);
+    T vz_z = p.cz[0] * (oz - at(p, vz, iz - 1, ix));
+    T vx_z = p.cz[0] * (at(p, vx, iz + 1, ix) - ox);
+    T vz_x = p.cx[0] * (at(p, vz, iz, ix + 1) - oz);
+    T vx_x = p.cx[0] * (ox - at(p, vx, iz, ix - 1));
+#pragma unroll
+    for (int k = 2; k <= NS; k++) {
+        vz_z += p.cz[k - 1] * (at(p, vz, iz + k - 1, ix) - at(p, vz, iz - k, ix));
+        vx_z += p.cz[k - 1] * (at(p, vx, iz + k, ix) - at(p, vx, iz - k + 1, ix));
+        vz_x += p.cx[k - 1] * (at(p, vz, iz, ix + k) - at(p, vz, iz, ix - (k - 1)));
+        vx_x += p.cx[k - 1] * (at(p, vx, iz, ix + k - 1) - at(p, vx, iz, ix - k));
+    }
+    const long long i = (long long)iz * p.pitch + ix;
+    T *szz = f + F_SZZ * p.plane, *szx = f + F_SZX * p.plane, *sxx = f + F_SXX * p.plane;
+    cpml_stress(p, bz, iz, ix, vz_z, vx_z, vz_x, vx_x);
+    stress_finish(p, szz, szx, sxx, iz, ix, i, szz[i], szx[i], sxx[i], p.c_lam[i], p.c_l2m[i],
+                  p.c_muzx[i], vz_z, vx_z, vz_x, vx_x);
+}
+
+// Whole velocity step of grid point (iz, ix) with checked loads: update when
+// it is interior, then the snapshot store / imaging of `slot`.
+template <typename T, int NS, int MODE>
+__device__ __forceinline__ void velocity_point(const StepParams<T> &p, int bz, int iz, int ix,
+                                               int slot)
+{
+    constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
+    T *f = p.fld + (long long)bz * p.shot_stride;
+    const T *szz = f + F_SZZ * p.plane, *szx = f + F_SZX * p.plane, *sxx = f + F_SXX * p.plane;
+    const T ozz = at(p, szz, iz, ix), ozx = at(p, szx, iz, ix), oxx = at(p, sxx, iz, ix);
+    const long long i = (long long)iz * p.pitch + ix;
+    T vzn = f[F_VZ * p.plane + i], vxn = f[F_VX * p.plane + i];
+    T uzn = U ? f[F_UZ * p.plane + i] : T(0), uxn = U ? f[F_UX * p.plane + i] : T(0);
+    if (iz >= p.nz1 && iz < p.nz2 && ix >= p.nx1 && ix < p.nx2) {
+        T szz_z = p.cz[0] * (at(p, szz, iz + 1, ix) - ozz);
+        T szx_z = p.cz[0] * (ozx - at(p, szx, iz - 1, ix));
+        T szx_x = p.cx[0] * (ozx - at(p, szx, iz, ix - 1));
+        T sxx_x = p.cx[0] * (at(p, sxx, iz, ix + 1) - oxx);
+#pragma unroll
+        for (int k = 2; k <= NS; k++) {
+            szz_z += p.cz[k - 1] * (at(p, szz, iz + k, ix) - at(p, szz, iz - k + 1, ix));
+            szx_z += p.cz[k - 1] * (at(p, szx, iz + k - 1, ix) - at(p, szx, iz - k, ix));
+            szx_x += p.cx[k - 1] * (at(p, szx, iz, ix + k - 1) - at(p, szx, iz, ix - k));
+            sxx_x += p.cx[k - 1] * (at(p, sxx, iz, ix + k) - at(p, sxx, iz, ix - (k - 1)));
+        }
+        cpml_velocity(p, bz, iz, ix, szz_z, szx_z, szx_x, sxx_x);
+        const T weo = MODE != MODE_FWD_NOWE ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i] : T(0);
+        velocity_finish<T, MODE>(p, f, i, vzn, vxn, uzn, uxn, weo, p.c_rz[i], p.c_rx[i], szz_z,
+                                 szx_z, szx_x, sxx_x, vzn, vxn, uzn, uxn);
+    }
+    if (slot >= 0)
+        snapshot_point<T, MODE>(p, bz, iz, ix, i, slot, ozz, ozx, oxx, vzn, vxn, uzn, uxn);
+}
+
 // ---------------------------------------------------------------------------
 // Stress step, direct loads: vdiff2 + pml_diff2 + update_s2 + surf_mirror
 // (src/cpu/n_kernel_lib_PSV.cpp:100-131, 134-205, 272-395).  Interior points

@@ -36,6 +36,13 @@ struct TileMaps {
 };
 int encode_tile_maps(TileMaps *m, const float *fld, int nfplanes, const float *coef, int nx, int nz,
                      int pitch, long long plane, int ns, int rpt);
+// Four-columns-per-thread kernels (FP32, psv_vec.cu): blocks of 32 x by
+// threads over 128 columns x by * rpt rows, rpt in {1, 2, 4}.
+cudaError_t launch_stress_v4(const StepParams<float> &p, int ns, int rpt, int by, int nbatch,
+                             cudaStream_t st);
+cudaError_t launch_velocity_v4(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
+                               int mode, int it, int slot, int rpt, int by, int nbatch,
+                               cudaStream_t st);
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
 cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,

@@ -126,15 +126,19 @@ public:
         const psv_grid &g = sv.g;
         const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
         const int al = 128 / (int)sizeof(T);
-        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_TMA)
-            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1 or 2");
-        if (opt.kernel_family == PSV_KERNELS_TMA && sizeof(T) != 4)
-            return fail(PSV_ERR_UNSUPPORTED, "TMA tile kernels are FP32 only");
+        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_VEC4)
+            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2 or 3");
+        if (opt.kernel_family >= PSV_KERNELS_TMA && sizeof(T) != 4)
+            return fail(PSV_ERR_UNSUPPORTED, "TMA and VEC4 kernels are FP32 only");
         if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
         if (opt.block_y > 0 || opt.rows_per_thread) opt.autotune = 0;  // explicit shape wins
         if (opt.kernel_family == PSV_KERNELS_TMA) {
             fam = PSV_KERNELS_TMA;
             rpt = tma_rpt(opt.rows_per_thread ? opt.rows_per_thread : 4);
+        } else if (opt.kernel_family == PSV_KERNELS_VEC4) {
+            fam = PSV_KERNELS_VEC4;
+            rpt = v4_rpt(opt.rows_per_thread ? opt.rows_per_thread : 1);
+            if (opt.block_y <= 0) blk = dim3(32, 4, 1);
         } else {
             rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
             if (opt.block_y <= 0) blk = dim3(32, 4, 1);
@@ -233,6 +237,7 @@ public:
     }
 
     static int tma_rpt(int r) { return (r == 2 || r == 4 || r == 8) ? r : 4; }
+    static int v4_rpt(int r) { return (r == 1 || r == 2 || r == 4) ? r : 1; }
 
     // Tensor maps of the field blocks for the TMA family (rebuilt when the
     // tile height or a field buffer changes).
@@ -254,19 +259,24 @@ public:
     // selects the checkpoint recompute state.
     cudaError_t ks(const StepParams<T> &s, bool second)
     {
-        if constexpr (sizeof(T) == 4)
+        if constexpr (sizeof(T) == 4) {
             if (fam == PSV_KERNELS_TMA)
                 return launch_stress_tma(s, second ? tmap2 : tmap, sv.ns, rpt, B, st);
+            if (fam == PSV_KERNELS_VEC4) return launch_stress_v4(s, sv.ns, rpt, (int)blk.y, B, st);
+        }
         (void)second;
         return launch_stress<T>(s, sv.ns, rpt, blk, B, st);
     }
     cudaError_t kv(const StepParams<T> &s, const SrcRecParams<T> &q, int mode, int it, int slot,
                    bool second)
     {
-        if constexpr (sizeof(T) == 4)
+        if constexpr (sizeof(T) == 4) {
             if (fam == PSV_KERNELS_TMA)
                 return launch_velocity_tma(s, q, second ? tmap2 : tmap, sv.ns, mode, it, slot, rpt,
                                            B, st);
+            if (fam == PSV_KERNELS_VEC4)
+                return launch_velocity_v4(s, q, sv.ns, mode, it, slot, rpt, (int)blk.y, B, st);
+        }
         (void)second;
         return launch_velocity<T>(s, q, sv.ns, mode, it, slot, rpt, blk, B, st);
     }
@@ -360,13 +370,13 @@ public:
     }
 
     // Sources and receivers bucketed by the velocity kernel's tiles (direct
-    // family: 32 columns x blk.y * |rpt| rows; TMA family: 64 x 4 rpt), so
-    // each block finds its own.
+    // family: 32 columns x blk.y * |rpt| rows; TMA: 64 x 4 rpt; VEC4: 128 x
+    // blk.y * rpt), so each block finds its own.
     int build_tile_index()
     {
         const int nshot = sv.s.nshot, nrec = sv.s.nrec;
-        const bool tma = fam == PSV_KERNELS_TMA;
-        const int tw = tma ? 64 : 32;
+        const bool tma = fam == PSV_KERNELS_TMA, v4 = fam == PSV_KERNELS_VEC4;
+        const int tw = tma ? 64 : v4 ? 128 : 32;
         const int tz = tma ? 4 * rpt : (int)blk.y * (rpt < 0 ? -rpt : rpt);
         const int ntx = (sv.g.nx + tw - 1) / tw, ntz = (sv.g.nz + tz - 1) / tz;
         const int nt_ = ntx * ntz;
@@ -1047,8 +1057,8 @@ public:
     // index, drops captured graphs).
     int set_shape(int f, int r, int by)
     {
-        if (f == PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
-        r = f == PSV_KERNELS_TMA ? tma_rpt(r) : rpt_ok<T>(r);
+        if (f >= PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
+        r = f == PSV_KERNELS_TMA ? tma_rpt(r) : f == PSV_KERNELS_VEC4 ? v4_rpt(r) : rpt_ok<T>(r);
         if (f == PSV_KERNELS_TMA) by = 4;
         if (f == fam && r == rpt && (int)blk.y == by) return PSV_OK;
         fam = f;
@@ -1086,15 +1096,18 @@ public:
         }
         // candidates: direct loads (rows per thread x block height), TMA tiles (rows per thread)
         std::vector<std::tuple<int, int, int>> cand;
-        if (opt.kernel_family != PSV_KERNELS_TMA) {
+        if (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_DIRECT) {
             const int r32[] = {1, 2, 4, -2, -4};
             for (int r : r32) {
                 if (sizeof(T) == 8 && r != 1) continue;
                 for (int by : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_DIRECT, r, by);
             }
         }
-        if (sizeof(T) == 4 && opt.kernel_family != PSV_KERNELS_DIRECT)
+        if (sizeof(T) == 4 && (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_TMA))
             for (int r : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_TMA, r, 4);
+        if (sizeof(T) == 4 && (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_VEC4))
+            for (int r : {1, 2, 4})
+                for (int by : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_VEC4, r, by);
         double best = 1e30;
         std::tuple<int, int, int> pick{fam, rpt, (int)blk.y};
         for (auto &c : cand) {

@@ -20,6 +20,9 @@ from . import _lib
 from ._lib import PsvOptions, check, dptr, f64, i32, iptr
 
 
+FAMILIES = {1: "direct", 2: "tma", 3: "vec4"}
+
+
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
             block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
             kernels="any") -> PsvOptions:
@@ -34,7 +37,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.checkpoint_interval = int(checkpoint_interval)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
-    o.kernel_family = {"any": 0, "direct": 1, "tma": 2}[kernels]
+    o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3}[kernels]
     return o
 
 
@@ -167,14 +170,14 @@ class Plan:
         block_y) with family "direct" or "tma"."""
         f, r, b = C.c_int(), C.c_int(), C.c_int()
         check(_lib.lib().psv_plan_autotune(self.h, int(nsteps), C.byref(f), C.byref(r), C.byref(b)))
-        return {1: "direct", 2: "tma"}[f.value], r.value, b.value
+        return FAMILIES[f.value], r.value, b.value
 
     @property
     def shape(self):
         """(family, rows_per_thread, block_y) of the kernels the plan launches now."""
         f, r, b = C.c_int(), C.c_int(), C.c_int()
         check(_lib.lib().psv_plan_shape(self.h, C.byref(f), C.byref(r), C.byref(b)))
-        return {1: "direct", 2: "tma"}[f.value], r.value, b.value
+        return FAMILIES[f.value], r.value, b.value
 
     def profile_kernels(self, nsteps=100):
         ms = np.zeros(6)

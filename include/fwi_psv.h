@@ -50,6 +50,7 @@ typedef enum {
 /* Time-step kernel families (psv_options.kernel_family). */
 #define PSV_KERNELS_DIRECT 1    /* per-thread loads of the stencil neighbours */
 #define PSV_KERNELS_TMA 2       /* tiles staged in shared memory by TMA tensor copies (FP32) */
+#define PSV_KERNELS_VEC4 3      /* four columns per thread, 128-bit loads and stores (FP32) */
 
 const char *psv_error_string(int status);
 /* Message of the last failing call on this host thread. */
@@ -128,9 +129,11 @@ typedef struct psv_options {
     int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
     int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
     int rows_per_thread;        /* rows each thread marches: direct family 1, 2, 4 (negative:
-                                   warp-shuffle variant); TMA family 2, 4, 8; 0 = default */
+                                   warp-shuffle variant); TMA family 2, 4, 8; VEC4 family
+                                   1, 2, 4; 0 = default */
     int kernel_family;          /* time-step kernels: 0 = any (the autotuner chooses),
-                                   PSV_KERNELS_DIRECT, PSV_KERNELS_TMA (FP32 only) */
+                                   PSV_KERNELS_DIRECT, PSV_KERNELS_TMA or PSV_KERNELS_VEC4
+                                   (the last two FP32 only) */
     int autotune;               /* 1 (default): time the tile-shape candidates on the first
                                    time loop and keep the fastest (psv_plan_autotune);
                                    0: use block_y / rows_per_thread as given */

@@ -28,7 +28,8 @@ def test_autotune_shape_and_parity(gpu, orc):
         p.set_observed(uz, ux)
         fam, rpt, by = p.autotune(8)
         assert (fam == "direct" and rpt in (1, 2, 4, -2, -4) and by in (2, 4, 8)) or \
-               (fam == "tma" and rpt in (2, 4, 8))
+               (fam == "tma" and rpt in (2, 4, 8)) or \
+               (fam == "vec4" and rpt in (1, 2, 4) and by in (2, 4, 8))
         assert p.shape == (fam, rpt, by)
         L2, g = p.gradient()
     assert L2 == pytest.approx(L2_ref, rel=1e-4)
@@ -37,7 +38,8 @@ def test_autotune_shape_and_parity(gpu, orc):
 
 
 SHAPES = [("direct", 2, 4), ("direct", 4, 2), ("direct", -2, 4), ("direct", -4, 8),
-          ("tma", 2, 0), ("tma", 4, 0), ("tma", 8, 0)]
+          ("tma", 2, 0), ("tma", 4, 0), ("tma", 8, 0),
+          ("vec4", 1, 4), ("vec4", 2, 2), ("vec4", 4, 8)]
 
 
 @pytest.mark.parametrize("fam,rpt,by", SHAPES)
@@ -57,17 +59,27 @@ def test_every_shape_gives_the_same_gradient(gpu, orc, fam, rpt, by, fdorder):
         assert helpers.rel_l2(b, a) < 1e-5
 
 
+@pytest.mark.parametrize("fam,rpt", [("tma", 4), ("vec4", 2)])
 @pytest.mark.parametrize("kw", [dict(fdorder=2, stencil="reference", nshot=3, nt=300),
                                 dict(fdorder=6, stencil="holberg", nshot=2, nt=250,
                                      imaging_sign=1),
                                 dict(fdorder=4, stencil="holberg", nshot=1, nt=250,
-                                     surf_offset=3)])
-def test_tma_family_against_oracle(gpu, orc, kw):
-    sv, true, init = helpers.case(nz=70, nx=130, **kw)
+                                     surf_offset=3),
+                                dict(fdorder=8, stencil="holberg", nshot=2, nt=450, nz=96,
+                                     nx=300)])
+def test_tiled_families_against_oracle(gpu, orc, kw, fam, rpt):
+    # The 96 x 300 case has plain blocks (interior, away from CPML and the
+    # surface) in both families.  Its data residual is 0.45 % of the traces:
+    # the FP32 gradient error against the oracle grows like the FP32 trace
+    # error divided by the relative residual, so a case whose waves have not
+    # yet reached the model perturbation (residual at round-off) cannot be
+    # compared at all.
+    kw = dict(dict(nz=70, nx=130), **kw)
+    sv, true, init = helpers.case(**kw)
     uz_ref, ux_ref = orc.simulate_fwd(sv, *true)
     L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz_ref, ux_ref)
-    with engine.Plan(sv, precision=32, kernels="tma", rows_per_thread=4) as p:
-        assert p.shape == ("tma", 4, 4)
+    with engine.Plan(sv, precision=32, kernels=fam, rows_per_thread=rpt) as p:
+        assert p.shape[:2] == (fam, rpt)
         p.set_model(*true)
         uz, ux = p.forward()
         assert helpers.rel_l2(uz, uz_ref) < 1e-5 and helpers.rel_l2(ux, ux_ref) < 1e-5
@@ -79,14 +91,15 @@ def test_tma_family_against_oracle(gpu, orc, kw):
         assert helpers.rel_l2(a, b) < 1e-4
 
 
-def test_tma_family_checkpointed_equals_full(gpu, orc):
+@pytest.mark.parametrize("fam", ["tma", "vec4"])
+def test_tiled_families_checkpointed_equals_full(gpu, orc, fam):
     sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, snap_dt=3)
     uz, ux = orc.simulate_fwd(sv, *true)
     out = []
     for storage in ("full", "checkpoint"):
-        with engine.Plan(sv, precision=32, kernels="tma", rows_per_thread=2,
+        with engine.Plan(sv, precision=32, kernels=fam, rows_per_thread=2,
                          storage=storage, checkpoint_interval=40) as p:
-            assert p.shape[0] == "tma"
+            assert p.shape[0] == fam
             p.set_model(*init)
             p.set_observed(uz, ux)
             out.append(p.gradient())
