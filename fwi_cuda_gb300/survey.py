@@ -245,11 +245,14 @@ def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml
 
 def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
                    stencil="holberg", npml=20, nrec=120, seed=1234, snap_dt=1, n_layers=5,
-                   vp_range=(1800.0, 3000.0), anomaly_radius=15, smooth_sigma=15.0, fc=100.0):
+                   vp_range=(1800.0, 3000.0), anomaly_radius=15, smooth_sigma=15.0, fc=100.0,
+                   surf_offset=None):
     """The 301 x 601 layered-plus-anomaly survey (one shot: forward + one
     adjoint gradient; eight shots: the FWI iteration case).  Smaller sizes
-    give the same structure for tests.  Returns (survey, true model, initial
-    model) with models as (lam, mu, rho)."""
+    give the same structure for tests.  surf_offset: free-surface row below
+    the frame (None: fdorder/2 rows, so the surface has mirrored rows above
+    it).  Returns (survey, true model, initial model) with models as
+    (lam, mu, rho)."""
     rng = np.random.default_rng(seed)
     fpad = fdorder // 2
     vp = layered_vp(nz, nx, n_layers, *vp_range, rng, top=2 * fpad)
@@ -260,5 +263,6 @@ def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
     rec_spacing = max(1, min(4, (nx - 2 * (npml + fpad) - 8) // max(nrec - 1, 1)))
     sv = surface_survey(nz, nx, dx, dx, nt, dt, fdorder=fdorder, stencil=stencil, npml=npml,
                         nshot=nshot, nrec=nrec, rec_spacing=rec_spacing, fc=fc,
-                        vp_max=float(vp.max()), snap_dt=snap_dt, seed=seed)
+                        vp_max=float(vp.max()), snap_dt=snap_dt, seed=seed,
+                        surf_offset=surf_offset)
     return sv, true, init
