@@ -63,7 +63,7 @@ def main():
         out[f"{name}/hist_szz"] = o["history"]["szz"][::25]
 
     # FWI: the reference's crosswell layout, CUDA-path sign (the CPU sign's
-    # search fails on physical cases), 3 iterations
+    # search fails on physical cases), 10 iterations
     sv, true, init = helpers.crosswell(nt=300, nz=51, nx=41, nshot=2, nrec=12, npml=8)
     mz, rz, rx, _ = ref.mat_av2(*true)
     uz = np.zeros((sv.nshot, sv.nrec, sv.nt))
@@ -71,7 +71,7 @@ def main():
     for s in range(sv.nshot):  # observed data: the reference's forward of the true model
         o = ref.kernel_PSV(sv, s, true[0], true[1], mz, rz, rx)
         uz[s], ux[s] = o["rtf_uz"], o["rtf_ux"]
-    r = ref.simulate_fwi(sv, *init, uz, ux, niter=3)
+    r = ref.simulate_fwi(sv, *init, uz, ux, niter=10)
     assert r["rc"] == 0
     name = "fwi_crosswell"
     pack(name, sv, out)

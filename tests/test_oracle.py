@@ -40,7 +40,7 @@ def test_fwi_iterations_match_golden_bitwise(orc, golden):
     name = "fwi_crosswell"
     sv = helpers.load_case(golden, name)
     r = orc.simulate_fwi(sv, *golden[f"{name}/init"], golden[f"{name}/obs_uz"],
-                         golden[f"{name}/obs_ux"], niter=3)
+                         golden[f"{name}/obs_ux"], niter=10)
     assert r["rc"] == 0
     for k in ("L2", "step", "lam", "mu", "rho", "grad_lam", "grad_mu", "grad_rho"):
         assert np.array_equal(r[k], golden[f"{name}/{k}"]), k
