@@ -294,6 +294,10 @@ def run_ours(args, rank, world):
             t0 = time.perf_counter()
             r = p.fwi_iteration(0.01)
             fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
+    batching = None
+    if rank == 0 and not args.no_batching:
+        shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by))
+        batching = batching_compare(sv, init, obs_uz, obs_ux, shape, nshot / (ms / 1e3))
 
     if rank != 0:
         return None
@@ -324,9 +328,66 @@ def run_ours(args, rank, world):
     if fwi:
         line["fwi_iteration_s"] = fwi["seconds"]
         line["fwi_trials"] = fwi["trials"]
+    if batching:
+        line["batching"] = batching
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
     return line
+
+
+def batching_compare(sv, init, obs_uz, obs_ux, shape, batched_shots_s):
+    """Shots/s of one FWI gradient along three paths on this GPU:
+    plain_dropin - the reference's per-shot structure through psv_kernel_PSV
+                   (kernel_PSV's interface): host model arrays, forward with
+                   the snapshot history returned to the host, host residual,
+                   adjoint fed the history back; shot 0 of the workload;
+    one_shot_plan - the plan with one shot per launch (device-resident);
+    checkpointed - the batched plan with checkpoint storage.
+    batched_vs_plain = the bench's batched shots/s / plain_dropin."""
+    from fwi_cuda_gb300 import engine, survey as S
+    lam, mu, rho = init
+    mz, rz, rx, _ = S.mat_av2(lam, mu, rho)
+    snap = (sv.snap_z1, sv.snap_z2, sv.snap_x1, sv.snap_x2, sv.snap_dt, sv.snap_dz, sv.snap_dx)
+    cz = (sv.a_z, sv.b_z, sv.K_z, sv.a_half_z, sv.b_half_z, sv.K_half_z)
+    cx = (sv.a_x, sv.b_x, sv.K_x, sv.a_half_x, sv.b_half_x, sv.K_half_x)
+
+    def call(grad, stf, src, nrec, history=None):
+        return engine.kernel_PSV(0, sv.nt, sv.nz, sv.nx, sv.dt, sv.dx, sv.dz, sv.surf, sv.isurf,
+                                 sv.hc, sv.fdorder, lam, mu, mz, rz, rx, grad, sv.pml_z, cz,
+                                 sv.pml_x, cx, len(src[0]), src[3], stf[0], stf[1], src[0],
+                                 src[1], src[2], nrec, sv.rtf_type, sv.z_rec, sv.x_rec,
+                                 not grad, snap, history=history, stencil=sv.stencil,
+                                 precision=32)
+
+    fire = np.asarray(sv.src_shot_to_fire)
+    own = np.nonzero(fire == 0)[0]
+    src0 = (np.asarray(sv.z_src)[own], np.asarray(sv.x_src)[own], np.zeros(len(own), np.int32),
+            sv.stf_type)
+    stf0 = (np.asarray(sv.stf_z)[own], np.asarray(sv.stf_x)[own])
+    t0 = time.perf_counter()
+    f = call(False, stf0, src0, sv.nrec)
+    res = (f["rtf_uz"] - obs_uz[0], f["rtf_ux"] - obs_ux[0])   # adjsrc2 residual
+    call(True, res, (sv.z_rec, sv.x_rec, np.zeros(sv.nrec, np.int32), sv.rtf_type), 0,
+         history=f["history"])
+    plain = 1.0 / (time.perf_counter() - t0)
+    del f
+
+    def plan_rate(**kw):
+        with engine.Plan(sv, precision=32, **shape, **kw) as p:
+            p.set_model(*init)
+            p.set_observed(obs_uz, obs_ux)
+            p.gradient(fetch=False)  # warm-up (graph capture)
+            t0 = time.perf_counter()
+            p.gradient(fetch=False)  # returns after the stream is idle
+            return sv.nshot / (time.perf_counter() - t0)
+
+    one = plan_rate(max_batch=1)
+    ck = plan_rate(storage="checkpoint")
+    return {"plain_dropin_shots_s": plain, "one_shot_plan_shots_s": one,
+            "checkpointed_shots_s": ck, "batched_shots_s": batched_shots_s,
+            "batched_vs_plain": batched_shots_s / plain,
+            "note": "plain_dropin: one shot through psv_kernel_PSV with the snapshot history "
+                    "on the host (host copies and layout conversion included)"}
 
 
 # ----------------------------------------------------------------------------- reference arm
@@ -353,6 +414,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--no-batching", action="store_true",
+                    help="skip the plain-vs-batched shots/s comparison")
     ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4"], default="auto",
                     help="time-step kernel family (auto: the plan's autotuner picks)")
     ap.add_argument("--rpt", type=int, default=0, help="rows per thread with --kernels")

@@ -266,3 +266,31 @@ def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
                         vp_max=float(vp.max()), snap_dt=snap_dt, seed=seed,
                         surf_offset=surf_offset)
     return sv, true, init
+
+
+def mat_av2(lam, mu, rho):
+    """Staggered material averages the reference's host computes before each
+    kernel_PSV call (mat_av2, src/cpu/n_kernel_lib_PSV.cpp:853-922): harmonic
+    mu at (z+1/2, x+1/2), reciprocal arithmetic rho at (z+1/2, x) and
+    (z, x+1/2), zero in the last row and column (left unset there by the
+    reference), and the model means C = (C_lam, C_mu, C_rho) over the other
+    cells.  The reference's vacuum test for rho_xp writes rho_zp
+    (:894-897); kept.  Returns (mu_zx, rho_zp, rho_xp, C)."""
+    lam, mu, rho = (np.asarray(a, np.float64) for a in (lam, mu, rho))
+    nz, nx = mu.shape
+    mu_zx, rho_zp, rho_xp = np.zeros((nz, nx)), np.zeros((nz, nx)), np.zeros((nz, nx))
+    m00, m01, m10, m11 = mu[:-1, :-1], mu[:-1, 1:], mu[1:, :-1], mu[1:, 1:]
+    with np.errstate(divide="ignore"):
+        v = 4.0 / ((1.0 / m00) + (1.0 / m01) + (1.0 / m10) + (1.0 / m11))
+    v[(m00 == 0) | (m01 == 0) | (m10 == 0) | (m11 == 0)] = 0.0
+    mu_zx[:-1, :-1] = v
+    r00, r10, r01 = rho[:-1, :-1], rho[1:, :-1], rho[:-1, 1:]
+    with np.errstate(divide="ignore"):
+        zp = 1.0 / (0.5 * (r00 + r10))
+        xp = 1.0 / (0.5 * (r00 + r01))
+    zp[(r00 < 1e-4) & (r10 < 1e-4)] = 0.0
+    zp[(r00 < 1e-4) & (r01 < 1e-4)] = 0.0
+    rho_zp[:-1, :-1], rho_xp[:-1, :-1] = zp, xp
+    n = (nz - 1) * (nx - 1)
+    C = np.array([lam[:-1, :-1].sum() / n, mu[:-1, :-1].sum() / n, rho[:-1, :-1].sum() / n])
+    return mu_zx, rho_zp, rho_xp, C

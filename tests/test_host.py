@@ -152,3 +152,15 @@ def test_options_reach_the_library_in_order():
     off = {n: getattr(_lib.PsvOptions, n).offset for n in fields}
     as_int = lambda n: int.from_bytes(raw[off[n]:off[n] + 4], "little", signed=True)
     assert as_int("kernel_family") == 2 and as_int("autotune") == 0 and as_int("rows_per_thread") == 8
+
+
+def test_host_mat_av2_matches_oracle(orc):
+    sv, true, _ = helpers.case(nz=41, nx=57)
+    lam, mu, rho = (a.copy() for a in true)
+    mu[5, 7] = 0.0  # vacuum cells take the reference's special cases
+    rho[9, 3] = rho[10, 3] = rho[9, 4] = 0.0
+    a = S.mat_av2(lam, mu, rho)
+    b = orc.mat_av2(lam, mu, rho)
+    for x, y in zip(a[:3], b[:3]):
+        assert np.array_equal(x, y)
+    assert np.allclose(a[3], b[3], rtol=1e-12)
