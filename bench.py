@@ -186,7 +186,10 @@ def run_profile(args):
     """One FWI gradient of a reduced case for ncu captures (--profile):
     nt / shots from --nt / --nshot; prints nothing measured."""
     from fwi_cuda_gb300 import engine
-    sv, true, init = workload(nt=args.nt, nshot=args.nshot)
+    if args.grid == "large":
+        sv, true, init = large_workload(nt=args.nt, nshot=args.nshot)
+    else:
+        sv, true, init = workload(nt=args.nt, nshot=args.nshot)
     with engine.Plan(sv, precision=32, **plan_kernels(args)) as p:
         p.set_model(*true)
         obs = p.forward()
@@ -294,6 +297,7 @@ def run_ours(args, rank, world):
             t0 = time.perf_counter()
             r = p.fwi_iteration(0.01)
             fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
+    large = large_grid(args) if rank == 0 and not args.no_large else None
     batching = None
     if rank == 0 and not args.no_batching:
         shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by))
@@ -330,6 +334,8 @@ def run_ours(args, rank, world):
         line["fwi_trials"] = fwi["trials"]
     if batching:
         line["batching"] = batching
+    if large:
+        line["large_grid"] = large
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
     return line
@@ -390,6 +396,58 @@ def batching_compare(sv, init, obs_uz, obs_ux, shape, batched_shots_s):
                     "on the host (host copies and layout conversion included)"}
 
 
+LARGE = dict(nz=1001, nx=2001, dx=0.5, nt=300, dt=2.5e-5, nshot=8, fdorder=8, npml=30,
+             nrec=500, snap_dt=3)
+
+
+def large_workload(nt=None, nshot=None):
+    from fwi_cuda_gb300 import survey as S
+    c = dict(LARGE)
+    c["nt"] = nt or c["nt"]
+    c["nshot"] = nshot or c["nshot"]
+    sv, true, init = S.config_layered(nz=c["nz"], nx=c["nx"], dx=c["dx"], nt=c["nt"], dt=c["dt"],
+                                      nshot=c["nshot"], fdorder=c["fdorder"], npml=c["npml"],
+                                      nrec=c["nrec"], snap_dt=c["snap_dt"], n_layers=8,
+                                      vp_range=(1500.0, 4500.0), seed=77, surf_offset=0)
+    sv.imaging_sign = 1
+    return sv, true, init
+
+
+def large_grid(args):
+    """Per-kernel bandwidth where the wavefields do not fit in L2: the
+    1001 x 2001, order-8 Holberg, 30-cell CPML grid of the batched-survey
+    configuration, 8 shots (577 MB of wavefields), time axis cropped to 300
+    steps.  Reports each kernel's algorithmic GB/s (the per-update bytes of
+    algorithmic_bytes x points / CUDA-event launch time) against the
+    measured HBM peak, and gradient throughput."""
+    from fwi_cuda_gb300 import engine
+    c = LARGE
+    sv, true, init = large_workload()
+    with engine.Plan(sv, precision=32, **plan_kernels(args)) as p:
+        p.set_model(*true)
+        obs = p.forward()
+        p.set_model(*init)
+        p.set_observed(*obs)
+        fam, rpt, by = p.autotune() if args.kernels == "auto" else p.shape
+        p.gradient(fetch=False)
+        t0 = time.perf_counter()
+        p.gradient(fetch=False)
+        sec = time.perf_counter() - t0
+        prof = p.profile_kernels(nsteps=100)
+    pts = c["nz"] * c["nx"] * c["nshot"]
+    peak, src = peaks()
+    kern = {}
+    for k, ms in prof.items():
+        alg = algorithmic_bytes(k, c["snap_dt"]) * pts
+        kern[k] = {"ms": round(ms, 4), "algorithmic_bytes": alg,
+                   "achieved_gbs": alg / (ms * 1e-3) / 1e9, "frac": alg / (ms * 1e-3) / 1e9 / peak}
+    return {"workload": "1001x2001, order-8 Holberg, 30-cell CPML, 8 shots, nt=300 (cropped), "
+                        "FP32, snap_dt=3", "kernels": {"family": fam, "rows_per_thread": rpt,
+                                                        "block_y": by},
+            "updates_per_s": 2.0 * pts * c["nt"] / sec, "gradient_s": sec,
+            "peak_gbs": peak, "peak_source": src, "per_kernel": kern}
+
+
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: each
@@ -414,6 +472,10 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--grid", choices=["bench", "large"], default="bench",
+                    help="--profile workload: the 301x601 bench grid or the 1001x2001 grid")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the 1001x2001 per-kernel bandwidth leg")
     ap.add_argument("--no-batching", action="store_true",
                     help="skip the plain-vs-batched shots/s comparison")
     ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4"], default="auto",

@@ -65,7 +65,22 @@ struct StepParams {
     long long gshot_shot_stride;
     const int *ctl;            // device [2]: global index of batch shot 0, shots in this batch
     int *err;                  // device error word (nonzero: a bounded wait gave up)
+    int nbatch;                // shots per launch (grid extent in shots)
 };
+
+// Block coordinates of the grid-stepping kernels: blockIdx.z = shot of the
+// batch, so x-adjacent tiles of one shot run together and share their halo
+// rows and columns through L1/L2.  (Making the shot the fastest index, so
+// the shots of one tile share the coefficients instead, measured 10-15 %
+// slower on L2-resident grids and no faster on HBM-bound ones for these
+// kernels; the persistent TMA kernels do order their tiles that way.)
+struct BlockPos {
+    int bz, bx, by, ntx;  // shot of the batch, tile column, tile row, tile columns
+};
+__device__ __forceinline__ BlockPos block_pos(int)
+{
+    return {(int)blockIdx.z, (int)blockIdx.x, (int)blockIdx.y, (int)gridDim.x};
+}
 
 // Source injection and receiver recording of one step for every shot of a batch.
 template <typename T>

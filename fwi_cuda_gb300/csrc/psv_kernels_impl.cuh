@@ -300,20 +300,36 @@ __device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRec
 // Rows [z0, z1) x columns [x0, x1) lie inside the interior, away from the
 // CPML strips: the velocity update there is a plain stencil.
 template <typename T>
-__device__ __forceinline__ bool plain_box(const StepParams<T> &p, int z0, int z1, int x0, int x1)
+__device__ __forceinline__ bool inner_box(const StepParams<T> &p, int z0, int z1, int x0, int x1)
 {
-    return z0 >= p.nz1 && z0 >= p.pz0 && z1 <= p.nz2 && z1 <= p.pz1 && x0 >= p.nx1 &&
-           x0 >= p.px0 && x1 <= p.nx2 && x1 <= p.px1 && p.plane < (1LL << 29);
+    return z0 >= p.nz1 && z1 <= p.nz2 && x0 >= p.nx1 && x1 <= p.nx2 && p.plane < (1LL << 29);
 }
 
-// ... and for the stress update also away from every free-surface row and
-// the rows / columns it mirrors (no cell of the box is written by another
-// thread's mirror, none of its threads writes a mirror).
+// Rows [z0, z1) x columns [x0, x1) have no CPML memory work.
 template <typename T>
-__device__ __forceinline__ bool plain_stress_box(const StepParams<T> &p, int z0, int z1, int x0,
+__device__ __forceinline__ bool cpml_free_box(const StepParams<T> &p, int z0, int z1, int x0, int x1)
+{
+    return z0 >= p.pz0 && z1 <= p.pz1 && x0 >= p.px0 && x1 <= p.px1;
+}
+
+// Rows [z0, z1) x columns [x0, x1) lie inside the interior (every stencil
+// neighbour inside the grid, 32-bit offsets suffice), away from the CPML
+// strips: the velocity update there is a plain stencil.
+template <typename T>
+__device__ __forceinline__ bool plain_box(const StepParams<T> &p, int z0, int z1, int x0, int x1)
+{
+    return inner_box(p, z0, z1, x0, x1) && cpml_free_box(p, z0, z1, x0, x1);
+}
+
+// Interior box the stress update may treat without free-surface work: away
+// from every free-surface row and the rows / columns it mirrors (no cell of
+// the box is written by another thread's mirror, none of its threads writes
+// a mirror).  CPML strips allowed.
+template <typename T>
+__device__ __forceinline__ bool inner_stress_box(const StepParams<T> &p, int z0, int z1, int x0,
                                                  int x1)
 {
-    bool ok = plain_box(p, z0, z1, x0, x1);
+    bool ok = inner_box(p, z0, z1, x0, x1);
     if (p.st) ok = ok && z0 > 2 * p.st - p.nz1;
     if (p.sb) ok = ok && z1 - 1 < 2 * p.sb - p.nz2;
     if (p.sl) ok = ok && x0 > 2 * p.sl - p.nx1;
@@ -321,32 +337,44 @@ __device__ __forceinline__ bool plain_stress_box(const StepParams<T> &p, int z0,
     return ok;
 }
 
+// ... and without CPML work: the plain stress stencil.
+template <typename T>
+__device__ __forceinline__ bool plain_stress_box(const StepParams<T> &p, int z0, int z1, int x0,
+                                                 int x1)
+{
+    return inner_stress_box(p, z0, z1, x0, x1) && cpml_free_box(p, z0, z1, x0, x1);
+}
+
 // Value of field plane `a` at (iz, ix), zero outside the grid (the values the
 // reference's padded arrays hold there).
-template <typename T>
+// CK = false: the caller guarantees (iz, ix) inside the grid (stencil
+// neighbours of interior points are), so the load is unchecked.
+template <typename T, bool CK = true>
 __device__ __forceinline__ T at(const StepParams<T> &p, const T *a, int iz, int ix)
 {
+    if constexpr (!CK) return a[(long long)iz * p.pitch + ix];
     return (iz >= 0 && iz < p.nz && ix >= 0 && ix < p.nx) ? a[(long long)iz * p.pitch + ix] : T(0);
 }
 
-// Whole stress update of interior point (iz, ix) of batch shot bz with
-// checked loads, the same operations as the kernels' unrolled windows.
-template <typename T, int NS>
+// Whole stress update of interior point (iz, ix) of batch shot bz, the same
+// operations as the kernels' unrolled windows.  CK: loads checked against
+// the grid (false only where every neighbour is known to be inside).
+template <typename T, int NS, bool CK = true>
 __device__ __forceinline__ void stress_point(const StepParams<T> &p, int bz, int iz, int ix)
 {
     T *f = p.fld + (long long)bz * p.shot_stride;
     const T *vz = f + F_VZ * p.plane, *vx = f + F_VX * p.plane;
-    const T oz = at(p, vz, iz, ix), ox = at(p, vx, iz, ix);
-    T vz_z = p.cz[0] * (oz - at(p, vz, iz - 1, ix));
-    T vx_z = p.cz[0] * (at(p, vx, iz + 1, ix) - ox);
-    T vz_x = p.cx[0] * (at(p, vz, iz, ix + 1) - oz);
-    T vx_x = p.cx[0] * (ox - at(p, vx, iz, ix - 1));
+    const T oz = at<T, CK>(p, vz, iz, ix), ox = at<T, CK>(p, vx, iz, ix);
+    T vz_z = p.cz[0] * (oz - at<T, CK>(p, vz, iz - 1, ix));
+    T vx_z = p.cz[0] * (at<T, CK>(p, vx, iz + 1, ix) - ox);
+    T vz_x = p.cx[0] * (at<T, CK>(p, vz, iz, ix + 1) - oz);
+    T vx_x = p.cx[0] * (ox - at<T, CK>(p, vx, iz, ix - 1));
 #pragma unroll
     for (int k = 2; k <= NS; k++) {
-        vz_z += p.cz[k - 1] * (at(p, vz, iz + k - 1, ix) - at(p, vz, iz - k, ix));
-        vx_z += p.cz[k - 1] * (at(p, vx, iz + k, ix) - at(p, vx, iz - k + 1, ix));
-        vz_x += p.cx[k - 1] * (at(p, vz, iz, ix + k) - at(p, vz, iz, ix - (k - 1)));
-        vx_x += p.cx[k - 1] * (at(p, vx, iz, ix + k - 1) - at(p, vx, iz, ix - k));
+        vz_z += p.cz[k - 1] * (at<T, CK>(p, vz, iz + k - 1, ix) - at<T, CK>(p, vz, iz - k, ix));
+        vx_z += p.cz[k - 1] * (at<T, CK>(p, vx, iz + k, ix) - at<T, CK>(p, vx, iz - k + 1, ix));
+        vz_x += p.cx[k - 1] * (at<T, CK>(p, vz, iz, ix + k) - at<T, CK>(p, vz, iz, ix - (k - 1)));
+        vx_x += p.cx[k - 1] * (at<T, CK>(p, vx, iz, ix + k - 1) - at<T, CK>(p, vx, iz, ix - k));
     }
     const long long i = (long long)iz * p.pitch + ix;
     T *szz = f + F_SZZ * p.plane, *szx = f + F_SZX * p.plane, *sxx = f + F_SXX * p.plane;
@@ -357,28 +385,28 @@ __device__ __forceinline__ void stress_point(const StepParams<T> &p, int bz, int
 
 // Whole velocity step of grid point (iz, ix) with checked loads: update when
 // it is interior, then the snapshot store / imaging of `slot`.
-template <typename T, int NS, int MODE>
+template <typename T, int NS, int MODE, bool CK = true>
 __device__ __forceinline__ void velocity_point(const StepParams<T> &p, int bz, int iz, int ix,
                                                int slot)
 {
     constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
     T *f = p.fld + (long long)bz * p.shot_stride;
     const T *szz = f + F_SZZ * p.plane, *szx = f + F_SZX * p.plane, *sxx = f + F_SXX * p.plane;
-    const T ozz = at(p, szz, iz, ix), ozx = at(p, szx, iz, ix), oxx = at(p, sxx, iz, ix);
+    const T ozz = at<T, CK>(p, szz, iz, ix), ozx = at<T, CK>(p, szx, iz, ix), oxx = at<T, CK>(p, sxx, iz, ix);
     const long long i = (long long)iz * p.pitch + ix;
     T vzn = f[F_VZ * p.plane + i], vxn = f[F_VX * p.plane + i];
     T uzn = U ? f[F_UZ * p.plane + i] : T(0), uxn = U ? f[F_UX * p.plane + i] : T(0);
     if (iz >= p.nz1 && iz < p.nz2 && ix >= p.nx1 && ix < p.nx2) {
-        T szz_z = p.cz[0] * (at(p, szz, iz + 1, ix) - ozz);
-        T szx_z = p.cz[0] * (ozx - at(p, szx, iz - 1, ix));
-        T szx_x = p.cx[0] * (ozx - at(p, szx, iz, ix - 1));
-        T sxx_x = p.cx[0] * (at(p, sxx, iz, ix + 1) - oxx);
+        T szz_z = p.cz[0] * (at<T, CK>(p, szz, iz + 1, ix) - ozz);
+        T szx_z = p.cz[0] * (ozx - at<T, CK>(p, szx, iz - 1, ix));
+        T szx_x = p.cx[0] * (ozx - at<T, CK>(p, szx, iz, ix - 1));
+        T sxx_x = p.cx[0] * (at<T, CK>(p, sxx, iz, ix + 1) - oxx);
 #pragma unroll
         for (int k = 2; k <= NS; k++) {
-            szz_z += p.cz[k - 1] * (at(p, szz, iz + k, ix) - at(p, szz, iz - k + 1, ix));
-            szx_z += p.cz[k - 1] * (at(p, szx, iz + k - 1, ix) - at(p, szx, iz - k, ix));
-            szx_x += p.cx[k - 1] * (at(p, szx, iz, ix + k - 1) - at(p, szx, iz, ix - k));
-            sxx_x += p.cx[k - 1] * (at(p, sxx, iz, ix + k) - at(p, sxx, iz, ix - (k - 1)));
+            szz_z += p.cz[k - 1] * (at<T, CK>(p, szz, iz + k, ix) - at<T, CK>(p, szz, iz - k + 1, ix));
+            szx_z += p.cz[k - 1] * (at<T, CK>(p, szx, iz + k - 1, ix) - at<T, CK>(p, szx, iz - k, ix));
+            szx_x += p.cx[k - 1] * (at<T, CK>(p, szx, iz, ix + k - 1) - at<T, CK>(p, szx, iz, ix - k));
+            sxx_x += p.cx[k - 1] * (at<T, CK>(p, sxx, iz, ix + k) - at<T, CK>(p, sxx, iz, ix - (k - 1)));
         }
         cpml_velocity(p, bz, iz, ix, szz_z, szx_z, szx_x, sxx_x);
         const T weo = MODE != MODE_FWD_NOWE ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i] : T(0);
@@ -397,13 +425,14 @@ __device__ __forceinline__ void velocity_point(const StepParams<T> &p, int bz, i
 template <typename T, int NS, int RPT, bool SH>
 __global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
 {
-    if ((int)blockIdx.z >= p.ctl[1]) return;
-    const int ix = p.nx1 + blockIdx.x * 32 + threadIdx.x;
-    const int zb = p.nz1 + (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
+    const BlockPos bp = block_pos(p.nbatch);
+    if (bp.bz >= p.ctl[1]) return;
+    const int ix = p.nx1 + bp.bx * 32 + threadIdx.x;
+    const int zb = p.nz1 + (bp.by * blockDim.y + threadIdx.y) * RPT;
     if (zb >= p.nz2) return;  // uniform across the warp; no block barrier follows
-    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
+    T *f = p.fld + (long long)bp.bz * p.shot_stride;
     {
-        const int bz0 = p.nz1 + blockIdx.y * blockDim.y * RPT, bx0 = p.nx1 + blockIdx.x * 32;
+        const int bz0 = p.nz1 + bp.by * blockDim.y * RPT, bx0 = p.nx1 + bp.bx * 32;
         if (plain_stress_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32)) {
             // no bounds, CPML or surface work: 32-bit offsets, unpredicated loads
             const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
@@ -483,7 +512,7 @@ __global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
         }
         if (iz >= p.nz2 || !colin) continue;
         const long long i = (long long)iz * P + ix;
-        cpml_stress(p, (int)blockIdx.z, iz, ix, vz_z, vx_z, vz_x, vx_x);
+        cpml_stress(p, bp.bz, iz, ix, vz_z, vx_z, vz_x, vx_x);
         stress_finish(p, szz, szx, sxx, iz, ix, i, szz[i], szx[i], sxx[i], p.c_lam[i], p.c_l2m[i],
                       p.c_muzx[i], vz_z, vx_z, vz_x, vx_x);
     }
@@ -504,17 +533,18 @@ template <typename T, int NS, int MODE, int RPT, bool SH>
 __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const SrcRecParams<T> q,
                                                   const int it, const int slot)
 {
-    if ((int)blockIdx.z >= p.ctl[1]) return;  // whole block
-    const int ix = blockIdx.x * 32 + threadIdx.x;
-    const int zb = (blockIdx.y * blockDim.y + threadIdx.y) * RPT;
+    const BlockPos bp = block_pos(p.nbatch);
+    if (bp.bz >= p.ctl[1]) return;  // whole block
+    const int ix = bp.bx * 32 + threadIdx.x;
+    const int zb = (bp.by * blockDim.y + threadIdx.y) * RPT;
     const long long P = p.pitch;
-    T *f = p.fld + (long long)blockIdx.z * p.shot_stride;
+    T *f = p.fld + (long long)bp.bz * p.shot_stride;
     const T *__restrict__ szz = f + F_SZZ * p.plane;
     const T *__restrict__ szx = f + F_SZX * p.plane;
     const T *__restrict__ sxx = f + F_SXX * p.plane;
     const bool colok = ix < p.nx;
     const bool colin = ix >= p.nx1 && ix < p.nx2;
-    const int bz0 = blockIdx.y * blockDim.y * RPT, bx0 = blockIdx.x * 32;
+    const int bz0 = bp.by * blockDim.y * RPT, bx0 = bp.bx * 32;
     const bool plain = plain_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32);
 
     if (plain) {  // interior, no CPML: 32-bit offsets, unpredicated loads
@@ -553,7 +583,7 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
                                      p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x, sxx_x, vzn, vxn,
                                      uzn, uxn);
             if (slot >= 0)
-                snapshot_point<T, MODE>(p, (int)blockIdx.z, zb + r, ix, i, slot, ozz, ozx, oxx,
+                snapshot_point<T, MODE>(p, bp.bz, zb + r, ix, i, slot, ozz, ozx, oxx,
                                         vzn, vxn, uzn, uxn);
         }
     } else if (zb < p.nz) {  // warp-uniform
@@ -597,7 +627,7 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
             const bool inner = colin && iz >= p.nz1 && iz < p.nz2;
             T vzn, vxn, uzn = T(0), uxn = T(0);
             if (inner) {
-                cpml_velocity(p, (int)blockIdx.z, iz, ix, szz_z, szx_z, szx_x, sxx_x);
+                cpml_velocity(p, bp.bz, iz, ix, szz_z, szx_z, szx_x, sxx_x);
                 constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
                 const T uzo = U ? f[F_UZ * p.plane + i] : T(0);
                 const T uxo = U ? f[F_UX * p.plane + i] : T(0);
@@ -616,11 +646,11 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
                 }
             }
             if (slot >= 0)
-                snapshot_point<T, MODE>(p, (int)blockIdx.z, iz, ix, i, slot, ozz, ozx, oxx, vzn,
+                snapshot_point<T, MODE>(p, bp.bz, iz, ix, i, slot, ozz, ozx, oxx, vzn,
                                         vxn, uzn, uxn);
         }
     }
-    srcrec_tile<T, MODE>(p, q, it, slot, blockIdx.y * gridDim.x + blockIdx.x, (int)blockIdx.z,
+    srcrec_tile<T, MODE>(p, q, it, slot, bp.by * bp.ntx + bp.bx, bp.bz,
                          threadIdx.y * 32 + threadIdx.x, 32 * blockDim.y);
 }
 

@@ -508,6 +508,7 @@ public:
         p.gshot_shot_stride = gshot_shot;
         p.ctl = ctl.as<int>();
         p.err = ctl.as<int>() + 2;
+        p.nbatch = B;
 
         SrcRecParams<T> q{};
         q.src_off = f_off.as<int>(); q.src_pos = f_pos.as<int>(); q.src_col = f_col.as<int>();

@@ -145,14 +145,17 @@ __device__ __forceinline__ bool wait_stage(uint32_t bar, uint32_t parity, int *e
 // Coefficient planes of StepParams::c_lam .. g2 in the coefficient tensor.
 enum { C_LAM = 0, C_L2M, C_MUZX, C_RZ, C_RX, C_G1, C_G2 };
 
-// Tile t of a launch: shot bz of the batch, origin (z0, x0).
+// Tile t of a launch: shot bz of the batch, origin (z0, x0).  The shot
+// varies fastest (t = spatial tile * nvalid + shot), so the tiles of one
+// place for all shots are processed together and share its coefficients
+// through L2.
 struct Tile {
     int bz, z0, x0;
 };
-__device__ __forceinline__ Tile tile_of(int t, int ntx, int ntz, int tz)
+__device__ __forceinline__ Tile tile_of(int t, int ntx, int nvalid, int tz)
 {
-    const int per = ntx * ntz, r = t % per;
-    return {t / per, (r / ntx) * tz, (r % ntx) * TW};
+    const int r = t / nvalid;
+    return {t % nvalid, (r / ntx) * tz, (r % ntx) * TW};
 }
 
 // ------------------------------------------------------------------ stress
@@ -405,7 +408,7 @@ __global__ void __launch_bounds__(NTHREADS) k_stress_tma(const StepParams<float>
         for (int s = 0; s < NSTAGE; s++) {
             const int t = blockIdx.x + s * gridDim.x;
             if (t < ntile)
-                stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(t, ntx, ntz, TZ), pps);
+                stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(t, ntx, p.ctl[1], TZ), pps);
         }
     }
     __syncthreads();  // barriers initialised before anyone polls them
@@ -414,12 +417,12 @@ __global__ void __launch_bounds__(NTHREADS) k_stress_tma(const StepParams<float>
         if (t >= ntile) break;
         const int s = k % NSTAGE;
         if (!wait_stage(stage_bar(stg, SF, s), (k / NSTAGE) & 1, p.err)) return;
-        stress_tile<NS, R>(p, stg + s * SF, tile_of(t, ntx, ntz, TZ));
+        stress_tile<NS, R>(p, stg + s * SF, tile_of(t, ntx, p.ctl[1], TZ));
         __syncthreads();  // stage s is read
         const int tn = t + NSTAGE * gridDim.x;
         if (threadIdx.x == 0 && tn < ntile) {
             fence_async_smem();
-            stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(tn, ntx, ntz, TZ), pps);
+            stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(tn, ntx, p.ctl[1], TZ), pps);
         }
     }
 }
@@ -449,7 +452,7 @@ __global__ void __launch_bounds__(NTHREADS) k_velocity_tma(const StepParams<floa
             const int t = blockIdx.x + s * gridDim.x;
             if (t < ntile)
                 velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s),
-                                            tile_of(t, ntx, ntz, TZ), pps, image);
+                                            tile_of(t, ntx, p.ctl[1], TZ), pps, image);
         }
     }
     __syncthreads();  // barriers initialised before anyone polls them
@@ -458,14 +461,14 @@ __global__ void __launch_bounds__(NTHREADS) k_velocity_tma(const StepParams<floa
         if (t >= ntile) break;
         const int s = k % NSTAGE;
         if (!wait_stage(stage_bar(stg, SF, s), (k / NSTAGE) & 1, p.err)) return;
-        const Tile T = tile_of(t, ntx, ntz, TZ);
+        const Tile T = tile_of(t, ntx, p.ctl[1], TZ);
         velocity_tile<NS, MODE, R>(p, stg + s * SF, T, slot);
         __syncthreads();  // stage s is read; the tile's velocities are written
         const int tn = t + NSTAGE * gridDim.x;
         if (threadIdx.x == 0 && tn < ntile) {
             fence_async_smem();
             velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s),
-                                        tile_of(tn, ntx, ntz, TZ), pps, image);
+                                        tile_of(tn, ntx, p.ctl[1], TZ), pps, image);
         }
         srcrec_tile<float, MODE>(p, q, it, slot, (T.z0 / TZ) * ntx + T.x0 / TW, T.bz,
                                  (int)threadIdx.x, NTHREADS);

@@ -11,9 +11,10 @@
 //     of its own,
 //   - reads and writes its own values and coefficients as float4,
 // so one 128-bit load serves four grid points and the per-thread set-up is
-// shared by 4 R points.  Threads whose points touch the CPML strips, free
-// surfaces or the grid frame run the checked per-point code of
-// psv_kernels_impl.cuh instead.
+// shared by 4 R points.  Threads in the CPML strips run the per-point code
+// of psv_kernels_impl.cuh with unchecked loads (every neighbour of an
+// interior point lies inside the grid); only threads whose points touch the
+// grid frame or a free surface check each load.
 // Both paths perform the same floating-point operations as the direct
 // kernels for every point.
 #include "psv_kernels_impl.cuh"
@@ -51,15 +52,16 @@ struct Row12 {
 template <int NS, int R>
 __global__ void __launch_bounds__(256) k_stress_v4(const StepParams<float> p)
 {
-    const int bz = blockIdx.z;
+    const BlockPos bp = block_pos(p.nbatch);
+    const int bz = bp.bz;
     if (bz >= p.ctl[1]) return;
     const int BY = blockDim.y;
-    const int x0 = blockIdx.x * VW, zb0 = blockIdx.y * BY * R;
+    const int x0 = bp.bx * VW, zb0 = bp.by * BY * R;
     const int x = x0 + 4 * threadIdx.x, zb = zb0 + threadIdx.y * R;
     float *f = p.fld + (long long)bz * p.shot_stride;
-    // per thread: only the threads whose 4 x R points touch the CPML strips,
-    // a free surface or the frame take the checked path
-    if (!plain_stress_box(p, zb, zb + R, x, x + 4)) {
+    // per thread: the threads whose 4 x R points touch the frame or a free
+    // surface take the checked path, CPML-strip threads the unchecked one
+    if (!inner_stress_box(p, zb, zb + R, x, x + 4)) {
 #pragma unroll 1
         for (int r = 0; r < R; r++) {
             const int iz = zb + r;
@@ -68,6 +70,13 @@ __global__ void __launch_bounds__(256) k_stress_v4(const StepParams<float> p)
             for (int c = 0; c < 4; c++)
                 if (x + c >= p.nx1 && x + c < p.nx2) stress_point<float, NS>(p, bz, iz, x + c);
         }
+        return;
+    }
+    if (!cpml_free_box(p, zb, zb + R, x, x + 4)) {  // CPML strips: unchecked point path
+#pragma unroll 1
+        for (int r = 0; r < R; r++)
+#pragma unroll 1
+            for (int c = 0; c < 4; c++) stress_point<float, NS, false>(p, bz, zb + r, x + c);
         return;
     }
     const int P = p.pitch, pl = (int)p.plane;
@@ -127,15 +136,16 @@ __global__ void __launch_bounds__(256) k_velocity_v4(const StepParams<float> p,
                                                      const SrcRecParams<float> q, const int it,
                                                      const int slot)
 {
-    const int bz = blockIdx.z;
+    const BlockPos bp = block_pos(p.nbatch);
+    const int bz = bp.bz;
     if (bz >= p.ctl[1]) return;  // whole block
     constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
     constexpr bool WE = MODE != MODE_FWD_NOWE;
     const int BY = blockDim.y;
-    const int x0 = blockIdx.x * VW, zb0 = blockIdx.y * BY * R;
+    const int x0 = bp.bx * VW, zb0 = bp.by * BY * R;
     const int x = x0 + 4 * threadIdx.x, zb = zb0 + threadIdx.y * R;
     float *f = p.fld + (long long)bz * p.shot_stride;
-    if (!plain_box(p, zb, zb + R, x, x + 4)) {  // per thread, as in the stress step
+    if (!inner_box(p, zb, zb + R, x, x + 4)) {  // per thread, as in the stress step
 #pragma unroll 1
         for (int r = 0; r < R; r++) {
             const int iz = zb + r;
@@ -144,6 +154,12 @@ __global__ void __launch_bounds__(256) k_velocity_v4(const StepParams<float> p,
             for (int c = 0; c < 4; c++)
                 if (x + c < p.nx) velocity_point<float, NS, MODE>(p, bz, iz, x + c, slot);
         }
+    } else if (!cpml_free_box(p, zb, zb + R, x, x + 4)) {  // CPML strips: unchecked points
+#pragma unroll 1
+        for (int r = 0; r < R; r++)
+#pragma unroll 1
+            for (int c = 0; c < 4; c++)
+                velocity_point<float, NS, MODE, false>(p, bz, zb + r, x + c, slot);
     } else {
         const int P = p.pitch, pl = (int)p.plane;
         const float *szz = f + F_SZZ * pl, *szx = f + F_SZX * pl, *sxx = f + F_SXX * pl;
@@ -208,7 +224,7 @@ __global__ void __launch_bounds__(256) k_velocity_v4(const StepParams<float> p,
                                                 oxx[c], vzn[c], vxn[c], uzn[c], uxn[c]);
         }
     }
-    srcrec_tile<float, MODE>(p, q, it, slot, blockIdx.y * gridDim.x + blockIdx.x, bz,
+    srcrec_tile<float, MODE>(p, q, it, slot, bp.by * bp.ntx + bp.bx, bz,
                              threadIdx.y * 32 + threadIdx.x, 32 * BY);
 }
 

@@ -20,7 +20,9 @@ def _grad(sv, init, uz, ux, **opt):
 
 
 def test_autotune_shape_and_parity(gpu, orc):
-    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, nz=81, nx=121)
+    # nt = 600: data residual 0.74 % of the traces (at nt = 300 it is 0.27 %
+    # and the FP32 gradient error, trace error / residual, sits at the bar)
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=600, nz=81, nx=121)
     uz, ux = orc.simulate_fwd(sv, *true)
     L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz, ux)
     with engine.Plan(sv, precision=32) as p:
