@@ -218,31 +218,49 @@ __device__ __forceinline__ void velocity_finish(const StepParams<T> &p, T *f, lo
         f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i] = weo + (vxn * vxn + vzn * vzn);
 }
 
+// Entries of one tile in the per-tile source / receiver index: sources to
+// inject [k0, k1) (index into t_src_k or t_rec_r, per src_kind) and
+// receivers to record [r0, r1) (empty when the pass records nothing).
+struct TileSR {
+    int k0, k1, r0, r1;
+};
+template <typename T>
+__device__ __forceinline__ TileSR tile_srcrec(const StepParams<T> &p, const SrcRecParams<T> &q,
+                                              int tile, int bz)
+{
+    TileSR s{0, 0, 0, 0};
+    if (q.src_kind == 0) {
+        const int *off = q.t_src_off + (long long)(p.ctl[0] + bz) * (q.ntiles + 1);
+        s.k0 = off[tile];
+        s.k1 = off[tile + 1];
+    } else if (q.src_kind == 1) {
+        s.k0 = q.t_rec_off[tile];
+        s.k1 = q.t_rec_off[tile + 1];
+    }
+    if (q.rtf_z) {
+        s.r0 = q.t_rec_off[tile];
+        s.r1 = q.t_rec_off[tile + 1];
+    }
+    return s;
+}
+
 // vsrc2 + urec2 (src/cpu/n_kernel_lib_PSV.cpp:487-576) for the sources and
 // receivers of one tile of the velocity kernel, after the tile's velocities
 // are written; then the snapshot fix-up of source cells (the stored
-// velocity is the post-injection one).  Called by every thread of the block.
+// velocity is the post-injection one).  Called by every thread of the block
+// with the tile's index entries `e`.
 template <typename T, int MODE>
-__device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRecParams<T> &q,
-                                            int it, int slot, int tile, int bz, int tid, int nth)
+__device__ __forceinline__ void srcrec_apply(const StepParams<T> &p, const SrcRecParams<T> &q,
+                                             int it, int slot, int bz, TileSR e, int tid, int nth)
 {
-    if (q.src_kind < 0 && !q.rtf_z) return;  // uniform: kernel argument
+    const int k0 = e.k0, k1 = e.k1;
+    const bool recs = e.r0 < e.r1;
+    if (k0 == k1 && !recs) return;  // uniform over the block
     const int shot = p.ctl[0] + bz;
     T *f = p.fld + (long long)bz * p.shot_stride;
     T *vz = f + F_VZ * p.plane;
     T *vx = f + F_VX * p.plane;
     const long long sp = p.snap_plane;
-    int k0 = 0, k1 = 0;
-    if (q.src_kind == 0) {
-        const int *off = q.t_src_off + (long long)shot * (q.ntiles + 1);
-        k0 = off[tile];
-        k1 = off[tile + 1];
-    } else if (q.src_kind == 1) {
-        k0 = q.t_rec_off[tile];
-        k1 = q.t_rec_off[tile + 1];
-    }
-    const bool recs = q.rtf_z && q.t_rec_off[tile] < q.t_rec_off[tile + 1];
-    if (k0 == k1 && !recs) return;  // uniform over the block
     __syncthreads();  // the tile's velocities are written
     const double sc = q.amp_scale[shot];
     const double *sz = q.stf_z + shot * q.stf_shot_stride + (long long)it * q.stf_ncol;
@@ -275,7 +293,7 @@ __device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRec
         double *rx = q.rtf_x + shot * q.rtf_shot_stride;
         const double ru = q.rec_unscale[shot];
         const long long row = (long long)it * q.nrec;
-        for (int k = q.t_rec_off[tile] + tid; k < q.t_rec_off[tile + 1]; k += nth) {
+        for (int k = e.r0 + tid; k < e.r1; k += nth) {
             const int rr = q.t_rec_r[k];
             const int pos = q.rec_pos[rr];
             const double pz = it ? rz[row - q.nrec + rr] : 0.0;
@@ -295,6 +313,15 @@ __device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRec
             h[H_VX * sp + c] = vx[pos] * p.inv_dt;
         }
     }
+}
+
+// srcrec_apply for tile `tile` of batch shot bz.
+template <typename T, int MODE>
+__device__ __forceinline__ void srcrec_tile(const StepParams<T> &p, const SrcRecParams<T> &q,
+                                            int it, int slot, int tile, int bz, int tid, int nth)
+{
+    if (q.src_kind < 0 && !q.rtf_z) return;  // uniform: kernel argument
+    srcrec_apply<T, MODE>(p, q, it, slot, bz, tile_srcrec(p, q, tile, bz), tid, nth);
 }
 
 // Rows [z0, z1) x columns [x0, x1) lie inside the interior, away from the

@@ -53,10 +53,10 @@ __host__ __device__ constexpr int stage_floats(int nh, int no, int ns, int r)
 }
 
 // Dynamic shared memory of a launch: NSTAGE stages, 128-byte aligned (TMA
-// destination rule), then one mbarrier per stage.
+// destination rule), then one mbarrier and one 32-byte tile record per stage.
 __host__ __device__ constexpr int pipe_smem_bytes(int nh, int no, int ns, int r)
 {
-    return NSTAGE * stage_floats(nh, no, ns, r) * 4 + 128 + 8 * NSTAGE;
+    return NSTAGE * stage_floats(nh, no, ns, r) * 4 + 128 + (8 + 32) * NSTAGE;
 }
 
 // Own planes the velocity step stages, per mode (after vz vx crz crx): We or
@@ -145,17 +145,22 @@ __device__ __forceinline__ bool wait_stage(uint32_t bar, uint32_t parity, int *e
 // Coefficient planes of StepParams::c_lam .. g2 in the coefficient tensor.
 enum { C_LAM = 0, C_L2M, C_MUZX, C_RZ, C_RX, C_G1, C_G2 };
 
-// Tile t of a launch: shot bz of the batch, origin (z0, x0).  The shot
-// varies fastest (t = spatial tile * nvalid + shot), so the tiles of one
-// place for all shots are processed together and share its coefficients
-// through L2.
+// Tile t of a launch: shot bz of the batch, origin (z0, x0), whether it is a
+// plain tile, and its source / receiver index entries.  The shot varies
+// fastest (t = spatial tile * nvalid + shot), so the tiles of one place for
+// all shots are processed together and share its coefficients through L2.
+// Thread 0 fills the record when it issues the tile's copies; the others
+// read it from shared memory after the stage barrier (one set of integer
+// divisions and index loads per tile, not per thread).
 struct Tile {
-    int bz, z0, x0;
+    int bz, z0, x0, plain;
+    TileSR sr;
 };
+static_assert(sizeof(Tile) == 32, "tile record size");
 __device__ __forceinline__ Tile tile_of(int t, int ntx, int nvalid, int tz)
 {
     const int r = t / nvalid;
-    return {t % nvalid, (r / ntx) * tz, (r % ntx) * TW};
+    return {t % nvalid, (r / ntx) * tz, (r % ntx) * TW, 0, {0, 0, 0, 0}};
 }
 
 // ------------------------------------------------------------------ stress
@@ -184,12 +189,11 @@ template <int NS, int R>
 __device__ __forceinline__ void stress_tile(const StepParams<float> &p, const float *st,
                                             const Tile &T)
 {
-    constexpr int TZ = 4 * R, HP = halo_plane(NS, R), OP = own_plane(R);
+    constexpr int HP = halo_plane(NS, R), OP = own_plane(R);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int lc = (w & 1) * 32 + lane, lr0 = (w >> 1) * R;
     const int x0 = T.x0, z0 = T.z0, ix = x0 + lc;
-    // plain tile: interior, no CPML, no free-surface row or mirror image
-    const bool plain = plain_stress_box(p, z0, z0 + TZ, x0, x0 + TW);
+    const bool plain = T.plain;  // interior, no CPML, no free-surface row or mirror image
 
     // derivatives of the thread's R rows, from shared memory only
     float dzz[R], dzx[R], dxz[R], dxx[R];  // vz_z, vz_x, vx_z, vx_x
@@ -291,7 +295,7 @@ template <int NS, int MODE, int R>
 __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const float *st,
                                               const Tile &T, int slot)
 {
-    constexpr int TZ = 4 * R, HP = halo_plane(NS, R), OP = own_plane(R);
+    constexpr int HP = halo_plane(NS, R), OP = own_plane(R);
     constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
     constexpr bool WE = MODE != MODE_FWD_NOWE;
     constexpr int K_WE = 4, K_U = WE ? 5 : 4, K_G = K_U + (U ? 2 : 0);
@@ -299,7 +303,7 @@ __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const 
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int lc = (w & 1) * 32 + lane, lr0 = (w >> 1) * R;
     const int x0 = T.x0, z0 = T.z0, ix = x0 + lc;
-    const bool plain = plain_box(p, z0, z0 + TZ, x0, x0 + TW);
+    const bool plain = T.plain;  // interior, no CPML
 
     float ozz[R], ozx[R], oxx[R], dzz[R], dzxz[R], dzxx[R], dxxx[R];
     {
@@ -386,6 +390,31 @@ __device__ __forceinline__ uint32_t stage_bar(float *stages, int sfl, int s)
     return smem_u32(reinterpret_cast<uint64_t *>(stages + NSTAGE * sfl) + s);
 }
 
+// Tile records of the NSTAGE stages (after the barriers).
+__device__ __forceinline__ Tile *stage_tile(float *stages, int sfl, int s)
+{
+    return reinterpret_cast<Tile *>(reinterpret_cast<uint64_t *>(stages + NSTAGE * sfl) + NSTAGE) + s;
+}
+
+template <int R>
+__device__ __forceinline__ Tile stress_record(const StepParams<float> &p, int t, int ntx)
+{
+    Tile T = tile_of(t, ntx, p.ctl[1], 4 * R);
+    T.plain = plain_stress_box(p, T.z0, T.z0 + 4 * R, T.x0, T.x0 + TW);
+    return T;
+}
+
+template <int R>
+__device__ __forceinline__ Tile velocity_record(const StepParams<float> &p,
+                                                const SrcRecParams<float> &q, int t, int ntx)
+{
+    Tile T = tile_of(t, ntx, p.ctl[1], 4 * R);
+    T.plain = plain_box(p, T.z0, T.z0 + 4 * R, T.x0, T.x0 + TW);
+    if (q.src_kind >= 0 || q.rtf_z)
+        T.sr = tile_srcrec(p, q, (T.z0 / (4 * R)) * ntx + T.x0 / TW, T.bz);
+    return T;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -407,22 +436,28 @@ __global__ void __launch_bounds__(NTHREADS) k_stress_tma(const StepParams<float>
         fence_init();
         for (int s = 0; s < NSTAGE; s++) {
             const int t = blockIdx.x + s * gridDim.x;
-            if (t < ntile)
-                stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(t, ntx, p.ctl[1], TZ), pps);
+            if (t < ntile) {
+                const Tile T = stress_record<R>(p, t, ntx);
+                *stage_tile(stg, SF, s) = T;
+                stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), T, pps);
+            }
         }
     }
-    __syncthreads();  // barriers initialised before anyone polls them
+    __syncthreads();  // barriers and records initialised before anyone reads them
     for (int k = 0;; k++) {
         const int t = blockIdx.x + k * gridDim.x;
         if (t >= ntile) break;
         const int s = k % NSTAGE;
         if (!wait_stage(stage_bar(stg, SF, s), (k / NSTAGE) & 1, p.err)) return;
-        stress_tile<NS, R>(p, stg + s * SF, tile_of(t, ntx, p.ctl[1], TZ));
-        __syncthreads();  // stage s is read
+        const Tile T = *stage_tile(stg, SF, s);
+        stress_tile<NS, R>(p, stg + s * SF, T);
+        __syncthreads();  // stage s and its record are read
         const int tn = t + NSTAGE * gridDim.x;
         if (threadIdx.x == 0 && tn < ntile) {
+            const Tile Tn = stress_record<R>(p, tn, ntx);
+            *stage_tile(stg, SF, s) = Tn;
             fence_async_smem();
-            stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), tile_of(tn, ntx, p.ctl[1], TZ), pps);
+            stress_issue<NS, R>(m, stg + s * SF, stage_bar(stg, SF, s), Tn, pps);
         }
     }
 }
@@ -450,28 +485,30 @@ __global__ void __launch_bounds__(NTHREADS) k_velocity_tma(const StepParams<floa
         fence_init();
         for (int s = 0; s < NSTAGE; s++) {
             const int t = blockIdx.x + s * gridDim.x;
-            if (t < ntile)
-                velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s),
-                                            tile_of(t, ntx, p.ctl[1], TZ), pps, image);
+            if (t < ntile) {
+                const Tile T = velocity_record<R>(p, q, t, ntx);
+                *stage_tile(stg, SF, s) = T;
+                velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s), T, pps, image);
+            }
         }
     }
-    __syncthreads();  // barriers initialised before anyone polls them
+    __syncthreads();  // barriers and records initialised before anyone reads them
     for (int k = 0;; k++) {
         const int t = blockIdx.x + k * gridDim.x;
         if (t >= ntile) break;
         const int s = k % NSTAGE;
         if (!wait_stage(stage_bar(stg, SF, s), (k / NSTAGE) & 1, p.err)) return;
-        const Tile T = tile_of(t, ntx, p.ctl[1], TZ);
+        const Tile T = *stage_tile(stg, SF, s);
         velocity_tile<NS, MODE, R>(p, stg + s * SF, T, slot);
-        __syncthreads();  // stage s is read; the tile's velocities are written
+        __syncthreads();  // stage s and its record are read; the tile's velocities are written
         const int tn = t + NSTAGE * gridDim.x;
         if (threadIdx.x == 0 && tn < ntile) {
+            const Tile Tn = velocity_record<R>(p, q, tn, ntx);
+            *stage_tile(stg, SF, s) = Tn;
             fence_async_smem();
-            velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s),
-                                        tile_of(tn, ntx, p.ctl[1], TZ), pps, image);
+            velocity_issue<NS, MODE, R>(m, stg + s * SF, stage_bar(stg, SF, s), Tn, pps, image);
         }
-        srcrec_tile<float, MODE>(p, q, it, slot, (T.z0 / TZ) * ntx + T.x0 / TW, T.bz,
-                                 (int)threadIdx.x, NTHREADS);
+        srcrec_apply<float, MODE>(p, q, it, slot, T.bz, T.sr, (int)threadIdx.x, NTHREADS);
     }
 }
 
