@@ -305,6 +305,30 @@ __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const 
     const int x0 = T.x0, z0 = T.z0, ix = x0 + lc;
     const bool plain = T.plain;  // interior, no CPML
 
+    // Imaging steps: issue the history and shot-gradient loads of all R rows
+    // first (they come from HBM), so their latency overlaps the stencil work.
+    float hv[R][5], gv[R][3];
+    long long qq[R];
+    bool win[R];
+    const long long sp = p.snap_plane;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        win[r] = false;
+        qq[r] = 0;
+        if (!image) continue;
+        const int iz = z0 + lr0 + r, dzr = iz - p.snap_z1, dxr = ix - p.snap_x1;
+        win[r] = !(dzr < 0 || iz > p.snap_z2 || dxr < 0 || ix > p.snap_x2) &&
+                 !(dzr % p.snap_dz) && !(dxr % p.snap_dx);
+        if (!win[r]) continue;
+        qq[r] = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
+        const float *h = p.hist + (long long)T.bz * p.hist_shot_stride +
+                         (long long)slot * p.hist_slot_stride + qq[r];
+        const float *g = p.gshot + (long long)T.bz * p.gshot_shot_stride + qq[r];
+        hv[r][0] = h[H_SZZ * sp]; hv[r][1] = h[H_SZX * sp]; hv[r][2] = h[H_SXX * sp];
+        hv[r][3] = h[H_VZ * sp]; hv[r][4] = h[H_VX * sp];
+        gv[r][0] = g[0]; gv[r][1] = g[sp]; gv[r][2] = g[2 * sp];
+    }
+
     float ozz[R], ozx[R], oxx[R], dzz[R], dzxz[R], dzxx[R], dxxx[R];
     {
         constexpr int W = R + 2 * NS - 1;
@@ -360,23 +384,17 @@ __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const 
                                          vzn, vxn, uzn, uxn);
         }
         if (slot < 0) continue;
-        if (image) {  // fwi_grad2 with the staged imaging factors
-            const int dzr = iz - p.snap_z1, dxr = ix - p.snap_x1;
-            if (dzr < 0 || iz > p.snap_z2 || dxr < 0 || ix > p.snap_x2) continue;
-            if (dzr % p.snap_dz || dxr % p.snap_dx) continue;
-            const long long sp = p.snap_plane;
-            const long long qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
-            const float *h = p.hist + (long long)T.bz * p.hist_shot_stride +
-                             (long long)slot * p.hist_slot_stride + qq;
-            const float fzz = h[H_SZZ * sp], fzx = h[H_SZX * sp], fxx = h[H_SXX * sp];
-            const float fvz = h[H_VZ * sp], fvx = h[H_VX * sp];
+        if (image) {  // fwi_grad2 with the staged imaging factors and preloaded history
+            if (!win[r]) continue;
+            const float fzz = hv[r][0], fzx = hv[r][1], fxx = hv[r][2];
+            const float fvz = hv[r][3], fvx = hv[r][4];
             const float s1 = o[k + K_G * OP] * ((fzz + fxx) * (ozz[r] + oxx[r]));
             const float s23 = o[k + (K_G + 1) * OP] *
                               (fzx * ozx[r] + 0.25f * ((fzz - fxx) * (ozz[r] - oxx[r])));
-            float *g = p.gshot + (long long)T.bz * p.gshot_shot_stride + qq;
-            g[0] -= s1;
-            g[sp] -= s23 + s1;
-            g[2 * sp] -= p.kimg * (uxn * fvx + uzn * fvz);
+            float *g = p.gshot + (long long)T.bz * p.gshot_shot_stride + qq[r];
+            g[0] = gv[r][0] - s1;
+            g[sp] = gv[r][1] - (s23 + s1);
+            g[2 * sp] = gv[r][2] - p.kimg * (uxn * fvx + uzn * fvz);
         } else {
             snapshot_point<float, MODE>(p, T.bz, iz, ix, i, slot, ozz[r], ozx[r], oxx[r], vzn, vxn,
                                         uzn, uxn);
