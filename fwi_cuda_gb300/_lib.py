@@ -102,6 +102,8 @@ SIGNATURES = {
     "psv_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip]),
     "psv_plan_shape": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "psv_multi_forward": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(_dp), C.POINTER(_dp)]),
+    "psv_multi_gradient": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _dp]),
     "psv_step_length": (C.c_int, [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp, C.c_int]),
     "psv_calc_opt_step": (C.c_double, [_dp, _dp]),
     "psv_kernel_PSV": (C.c_int,

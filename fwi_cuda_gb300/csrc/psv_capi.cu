@@ -3,6 +3,8 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "psv_plan.cuh"
 
@@ -134,6 +136,38 @@ int make_survey(const psv_grid *gp, const psv_shots *sp, Survey &out)
 
 using namespace psv;
 
+// Runs job(k) for every plan on its own host thread (the plans' streams run
+// concurrently on the device) and returns the first failure.
+template <typename F> static int run_plans(psv_plan *const *plans, int n, F job)
+{
+    if (!plans || n <= 0) return fail(PSV_ERR_ARG, "multi: need at least one plan");
+    for (int k = 0; k < n; k++) {
+        if (!plans[k] || !plans[k]->impl) return fail(PSV_ERR_ARG, "multi: null plan " + std::to_string(k));
+        for (int j = 0; j < k; j++)
+            if (plans[j] == plans[k]) return fail(PSV_ERR_ARG, "multi: plan listed twice");
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(PSV_ERR_CUDA, "multi: no current device");
+    std::vector<int> st(n, PSV_OK);
+    std::vector<std::string> msg(n);
+    std::vector<std::thread> th;
+    th.reserve(n);
+    for (int k = 0; k < n; k++)
+        th.emplace_back([&, k] {
+            if (cudaSetDevice(dev) != cudaSuccess) {
+                st[k] = PSV_ERR_CUDA;
+                msg[k] = "cudaSetDevice failed";
+                return;
+            }
+            st[k] = job(k);
+            if (st[k] != PSV_OK) msg[k] = psv_last_error();
+        });
+    for (auto &t : th) t.join();
+    for (int k = 0; k < n; k++)
+        if (st[k] != PSV_OK) return fail(st[k], "survey " + std::to_string(k) + ": " + msg[k]);
+    return PSV_OK;
+}
+
 extern "C" {
 
 const char *psv_error_string(int s)
@@ -235,6 +269,25 @@ int psv_gradient(psv_plan *p, double *L2, double *gl, double *gm, double *gr)
     PLAN_CHECK(p);
     PSV_TRY(p->impl->gradient(L2));
     if (gl || gm || gr) return p->impl->get_gradient(gl, gm, gr);
+    return PSV_OK;
+}
+
+int psv_multi_forward(psv_plan *const *plans, int n, double *const *uz, double *const *ux)
+{
+    return run_plans(plans, n, [&](int k) {
+        return plans[k]->impl->forward(uz ? uz[k] : nullptr, ux ? ux[k] : nullptr);
+    });
+}
+
+int psv_multi_gradient(psv_plan *const *plans, int n, double *L2)
+{
+    if (plans && n > 0)
+        for (int k = 0; k < n; k++)  // tune serially: concurrent work would distort the timings
+            if (plans[k] && plans[k]->impl) PSV_TRY(plans[k]->impl->prepare());
+    std::vector<double> l2(n > 0 ? n : 0, 0.0);
+    PSV_TRY(run_plans(plans, n, [&](int k) { return plans[k]->impl->gradient(&l2[k]); }));
+    if (L2)
+        for (int k = 0; k < n; k++) L2[k] = l2[k];
     return PSV_OK;
 }
 

@@ -1135,6 +1135,13 @@ public:
         if (by) *by = fam == PSV_KERNELS_TMA ? 4 : (int)blk.y;
     }
 
+    int prepare() override
+    {
+        if (!have_model || !have_obs) return PSV_OK;
+        PSV_TRY(ensure_hist());
+        return maybe_autotune();
+    }
+
     int maybe_autotune()
     {
         if (tuned || !opt.autotune || !have_model || !have_obs) return PSV_OK;

@@ -261,3 +261,26 @@ def simulate_PSV(workdir: str, max_iter: int = 0, imaging_sign: int = -1, **opts
     o = options(**opts)
     check(_lib.lib().psv_simulate_PSV(workdir.encode(), int(max_iter), int(imaging_sign),
                                       C.byref(o)))
+
+
+def multi_forward(plans):
+    """psv_multi_forward: forward modelling of several surveys (one Plan each,
+    uneven sizes allowed) concurrently; returns [(uz, ux)] per plan."""
+    n = len(plans)
+    hs = (C.c_void_p * n)(*[p.h for p in plans])
+    out = [(np.zeros((p.sv.nshot, p.sv.nrec, p.sv.nt)), np.zeros((p.sv.nshot, p.sv.nrec, p.sv.nt)))
+           for p in plans]
+    uz = (_lib._dp * n)(*[dptr(o[0]) for o in out])
+    ux = (_lib._dp * n)(*[dptr(o[1]) for o in out])
+    check(_lib.lib().psv_multi_forward(hs, n, uz, ux))
+    return out
+
+
+def multi_gradient(plans):
+    """psv_multi_gradient: one FWI gradient of every survey (one Plan each)
+    concurrently; returns L2 per plan, gradients stay on the plans."""
+    n = len(plans)
+    hs = (C.c_void_p * n)(*[p.h for p in plans])
+    L2 = np.zeros(n)
+    check(_lib.lib().psv_multi_gradient(hs, n, dptr(L2)))
+    return L2

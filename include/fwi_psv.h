@@ -173,6 +173,21 @@ int psv_forward(psv_plan *plan, double *rtf_uz, double *rtf_ux);
  * global gradients after the call. */
 int psv_gradient(psv_plan *plan, double *L2, double *grad_lam, double *grad_mu,
                  double *grad_rho);
+
+/* Several surveys at once (uneven grid sizes, time-step counts and stencil
+ * orders: one plan each, all created on the calling thread's current
+ * device).  Runs psv_forward / psv_gradient of every plan concurrently, each
+ * on its plan's own stream and host thread, so the GPU overlaps the surveys'
+ * time loops; one call, not one kernel launch.  Plans still due an autotune
+ * are tuned one after another first, so their timings are not disturbed.
+ * The same plan may not appear twice.  forward: uz[k], ux[k] as in
+ * psv_forward for plan k (entries may be NULL); gradient: L2[k] per plan
+ * (may be NULL), the global gradients stay on each plan (psv_get_gradient).
+ * The first failing plan's status is returned, its message prefixed with its
+ * index.  No counterpart in the reference (one survey per program run). */
+int psv_multi_forward(psv_plan *const *plans, int nplans, double *const *rtf_uz,
+                      double *const *rtf_ux);
+int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
 int psv_reset_gradient(psv_plan *plan);
 int psv_get_gradient(psv_plan *plan, double *grad_lam, double *grad_mu, double *grad_rho);
 int psv_set_gradient(psv_plan *plan, const double *grad_lam, const double *grad_mu,
