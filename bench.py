@@ -298,6 +298,7 @@ def run_ours(args, rank, world):
             r = p.fwi_iteration(0.01)
             fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
     large = large_grid(args) if rank == 0 and not args.no_large else None
+    uneven = uneven_batch(args) if rank == 0 and not args.no_uneven else None
     batching = None
     if rank == 0 and not args.no_batching:
         shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by))
@@ -336,6 +337,8 @@ def run_ours(args, rank, world):
         line["batching"] = batching
     if large:
         line["large_grid"] = large
+    if uneven:
+        line["uneven_batch"] = uneven
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
     return line
@@ -448,6 +451,49 @@ def large_grid(args):
             "peak_gbs": peak, "peak_source": src, "per_kernel": kern}
 
 
+UNEVEN = [  # (nz, nx, nt cropped, fdorder, npml, peak Hz): the uneven-batch grids, 4 shots each
+    (401, 801, 200, 4, 20, 60.0), (601, 1201, 300, 8, 30, 80.0),
+    (1001, 2001, 400, 4, 30, 100.0), (1501, 3001, 600, 8, 40, 120.0)]
+
+
+def uneven_batch(args):
+    """Four surveys of the uneven-batch configuration's grid sizes (4 shots
+    each, time axes cropped to 200-600 steps, orders 4 and 8 mixed, CPML 20-40
+    cells, Ricker peaks 60-120 Hz): one FWI gradient of all four through
+    psv_multi_gradient (concurrent) against the same plans one after another."""
+    from fwi_cuda_gb300 import engine, survey as S
+    plans, pts = [], 0.0
+    try:
+        for k, (nz, nx, nt, fd, npml, fc) in enumerate(UNEVEN):
+            sv, true, init = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=4,
+                                              fdorder=fd, npml=npml, nrec=200, snap_dt=3,
+                                              fc=fc, seed=100 + k, surf_offset=0)
+            sv.imaging_sign = 1
+            p = engine.Plan(sv, precision=32, hbm_budget_gb=40.0, **plan_kernels(args))
+            plans.append(p)
+            p.set_model(*true)
+            obs = p.forward()
+            p.set_model(*init)
+            p.set_observed(*obs)
+            pts += 2.0 * 4 * nt * nz * nx
+        engine.multi_gradient(plans)  # tunes and captures graphs
+        t0 = time.perf_counter()
+        engine.multi_gradient(plans)
+        conc = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for p in plans:
+            p.gradient(fetch=False)
+        seq = time.perf_counter() - t0
+        return {"workload": "4 surveys: 401x801 (nt 200), 601x1201 (300), 1001x2001 (400), "
+                            "1501x3001 (600), 4 shots each, orders 4/8, FP32",
+                "concurrent_s": conc, "sequential_s": seq,
+                "concurrent_updates_per_s": pts / conc, "sequential_updates_per_s": pts / seq,
+                "kernels": [dict(zip(("family", "rows_per_thread", "block_y"), p.shape)) for p in plans]}
+    finally:
+        for p in plans:
+            p.close()
+
+
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: each
@@ -474,6 +520,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--grid", choices=["bench", "large"], default="bench",
                     help="--profile workload: the 301x601 bench grid or the 1001x2001 grid")
+    ap.add_argument("--no-uneven", action="store_true",
+                    help="skip the four-survey uneven-batch leg")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 1001x2001 per-kernel bandwidth leg")
     ap.add_argument("--no-batching", action="store_true",
