@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(NTHREADS) k_stress_tma(const StepParams<float>
 // sources and receivers.
 // ---------------------------------------------------------------------------
 template <int NS, int MODE, int R>
-__global__ void __launch_bounds__(NTHREADS) k_velocity_tma(const StepParams<float> p,
+__global__ void __launch_bounds__(NTHREADS, 3) k_velocity_tma(const StepParams<float> p,
                                                            const SrcRecParams<float> q,
                                                            const int it, const int slot,
                                                            const __grid_constant__ TileMaps m)
