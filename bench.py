@@ -494,6 +494,61 @@ def uneven_batch(args):
             p.close()
 
 
+FULL = {  # the batched-survey and the large single-model configurations
+    "c3": dict(nz=1001, nx=2001, dx=0.5, dt=2.5e-5, nt=10000, nshot=64, nrec=500, rec_spacing=3,
+               fdorder=8, npml=30, layers=8, dip=60.0, fault=None, anomalies=6, radius=(10, 30),
+               checkpoint_interval=157),   # 64 checkpoints per shot
+    "c5": dict(nz=2001, nx=4001, dx=1.0, dt=1e-4, nt=12000, nshot=32, nrec=800, rec_spacing=4,
+               fdorder=8, npml=40, layers=8, dip=40.0, fault=(2000, 40), anomalies=10,
+               radius=(10, 30), checkpoint_interval=0),  # checkpoints sized to the 180 GB budget
+}
+
+
+def run_full_config(args):
+    """One FWI gradient of a full configuration (--config c3 | c5): seeded
+    dipping layered model (vp in [1500, 4500] m/s, Gardner rho, vs = vp/1.73,
+    c5 with a fault), +-10 % Gaussian anomalies, initial model smoothed with
+    sigma = 15 cells, surface sources and receivers, checkpointed storage.
+    Prints one JSON line: seconds per gradient, forward + adjoint updates/s
+    (the recomputed forward is extra work, not counted), shots/s."""
+    import numpy as np
+    from fwi_cuda_gb300 import engine, survey as S
+    c = FULL[args.config]
+    rng = np.random.default_rng(2024)
+    fpad = c["fdorder"] // 2
+    vp = S.layered_vp(c["nz"], c["nx"], c["layers"], 1500.0, 4500.0, rng, dip_cells=c["dip"],
+                      top=2 * fpad, fault=c["fault"])
+    vp = S.add_anomalies(vp, rng, c["anomalies"], amp=0.10, radius=c["radius"], signs=(1, -1),
+                         margin=c["npml"] + fpad)
+    true, init = S.model_from_vp(vp), S.smoothed(vp, 15.0)
+    sv = S.surface_survey(c["nz"], c["nx"], c["dx"], c["dx"], c["nt"], c["dt"],
+                          fdorder=c["fdorder"], npml=c["npml"], nshot=c["nshot"], nrec=c["nrec"],
+                          rec_spacing=c["rec_spacing"], fc=100.0, vp_max=float(vp.max()),
+                          snap_dt=3, surf_offset=0, seed=7)
+    sv.imaging_sign = 1
+    t0 = time.perf_counter()
+    with engine.Plan(sv, precision=32, storage="checkpoint",
+                     checkpoint_interval=c["checkpoint_interval"], **plan_kernels(args)) as p:
+        p.set_model(*true)
+        obs = p.forward()
+        t_obs = time.perf_counter() - t0
+        p.set_model(*init)
+        p.set_observed(*obs)
+        fam, rpt, by = p.autotune() if args.kernels == "auto" else p.shape
+        t1 = time.perf_counter()
+        L2, _ = p.gradient(fetch=False)
+        sec = time.perf_counter() - t1
+        tm = p.timing()
+        mem = p.device_bytes
+    upd = 2.0 * c["nshot"] * c["nt"] * c["nz"] * c["nx"]
+    print(json.dumps({"config": args.config, "workload": {k: v for k, v in c.items()},
+                      "kernels": {"family": fam, "rows_per_thread": rpt, "block_y": by},
+                      "gradient_s": sec, "updates_per_s_fwd_adj": upd / sec,
+                      "shots_per_s": c["nshot"] / sec, "forward_ms": tm["forward_ms"],
+                      "adjoint_ms": tm["adjoint_ms"], "observed_data_s": t_obs,
+                      "device_gb": mem / 1e9, "L2": L2, "finite": bool(np.isfinite(L2))}))
+
+
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: each
@@ -520,6 +575,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--grid", choices=["bench", "large"], default="bench",
                     help="--profile workload: the 301x601 bench grid or the 1001x2001 grid")
+    ap.add_argument("--config", choices=["c3", "c5"], default=None,
+                    help="run one gradient of a full configuration instead of the bench")
     ap.add_argument("--no-uneven", action="store_true",
                     help="skip the four-survey uneven-batch leg")
     ap.add_argument("--no-large", action="store_true",
@@ -539,6 +596,8 @@ def main():
     ap.add_argument("--nt", type=int, default=400, help="time steps of the --profile case")
     ap.add_argument("--nshot", type=int, default=2, help="shots of the --profile case")
     args = ap.parse_args()
+    if args.config:
+        return run_full_config(args)
     if args.profile:
         run_profile(args)
         return
