@@ -194,6 +194,51 @@ __device__ __forceinline__ void snapshot_point(const StepParams<T> &p, int shot,
     }
 }
 
+// fwi_grad2 of one point split in two: image_preload issues the point's
+// history, shot-gradient and imaging-factor loads (they come from HBM) as
+// early as the caller wants; image_apply then performs snapshot_point's
+// adjoint operations with them.
+template <typename T>
+struct ImagePre {
+    T h[5], g[3], g1, g2;
+    long long qq;
+    bool in;
+};
+template <typename T>
+__device__ __forceinline__ ImagePre<T> image_preload(const StepParams<T> &p, int bz, int iz, int ix,
+                                                     long long i, int slot)
+{
+    ImagePre<T> e{};
+    const int dzr = iz - p.snap_z1, dxr = ix - p.snap_x1;
+    e.in = !(dzr < 0 || iz > p.snap_z2 || dxr < 0 || ix > p.snap_x2) && !(dzr % p.snap_dz) &&
+           !(dxr % p.snap_dx);
+    if (!e.in) return e;
+    const long long sp = p.snap_plane;
+    e.qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
+    const T *h = p.hist + (long long)bz * p.hist_shot_stride + (long long)slot * p.hist_slot_stride + e.qq;
+    const T *g = p.gshot + (long long)bz * p.gshot_shot_stride + e.qq;
+    e.h[0] = h[H_SZZ * sp]; e.h[1] = h[H_SZX * sp]; e.h[2] = h[H_SXX * sp];
+    e.h[3] = h[H_VZ * sp]; e.h[4] = h[H_VX * sp];
+    e.g[0] = g[0]; e.g[1] = g[sp]; e.g[2] = g[2 * sp];
+    e.g1 = p.g1[i];
+    e.g2 = p.g2[i];
+    return e;
+}
+template <typename T>
+__device__ __forceinline__ void image_apply(const StepParams<T> &p, int bz, const ImagePre<T> &e,
+                                            T ozz, T ozx, T oxx, T uzn, T uxn)
+{
+    if (!e.in) return;
+    const long long sp = p.snap_plane;
+    const T fzz = e.h[0], fzx = e.h[1], fxx = e.h[2], fvz = e.h[3], fvx = e.h[4];
+    const T s1 = e.g1 * ((fzz + fxx) * (ozz + oxx));
+    const T s23 = e.g2 * (fzx * ozx + T(0.25) * ((fzz - fxx) * (ozz - oxx)));
+    T *g = p.gshot + (long long)bz * p.gshot_shot_stride + e.qq;
+    g[0] = e.g[0] - s1;
+    g[sp] = e.g[1] - (s23 + s1);
+    g[2 * sp] = e.g[2] - p.kimg * (uxn * fvx + uzn * fvz);
+}
+
 // update_v2 (src/cpu/n_kernel_lib_PSV.cpp:243-270) of interior point i from
 // its old velocities, plus the displacement integration (adjoint and the
 // drop-in forward) and the energy sum We / We_adj from the old u / We
@@ -581,6 +626,11 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
         const T *__restrict__ zxc = f + F_SZX * pl + i0;
         const T *__restrict__ xxc = f + F_SXX * pl + i0;
         constexpr int W = RPT + 2 * NS - 1;
+        const bool image = MODE == MODE_ADJ && slot >= 0;
+        ImagePre<T> pre[RPT];  // imaging loads first: their latency overlaps the stencil loads
+#pragma unroll
+        for (int r = 0; r < RPT; r++)
+            if (image) pre[r] = image_preload(p, bp.bz, zb + r, ix, i0 + r * P, slot);
         T wzz[W], wzx[W];  // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
 #pragma unroll
         for (int j = 0; j < W; j++) {
@@ -609,7 +659,9 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
             velocity_finish<T, MODE>(p, f, i, f[F_VZ * pl + i], f[F_VX * pl + i], uzo, uxo, weo,
                                      p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x, sxx_x, vzn, vxn,
                                      uzn, uxn);
-            if (slot >= 0)
+            if (image)
+                image_apply(p, bp.bz, pre[r], ozz, ozx, oxx, uzn, uxn);
+            else if (slot >= 0)
                 snapshot_point<T, MODE>(p, bp.bz, zb + r, ix, i, slot, ozz, ozx, oxx,
                                         vzn, vxn, uzn, uxn);
         }
