@@ -508,7 +508,8 @@ def run_full_config(args):
     """One FWI gradient of a full configuration (--config c3 | c5): seeded
     dipping layered model (vp in [1500, 4500] m/s, Gardner rho, vs = vp/1.73,
     c5 with a fault), +-10 % Gaussian anomalies, initial model smoothed with
-    sigma = 15 cells, surface sources and receivers, checkpointed storage.
+    sigma = 15 cells, surface sources and receivers, checkpointed storage
+    (two-level, or binomial with --storage binomial).
     Prints one JSON line: seconds per gradient, forward + adjoint updates/s
     (the recomputed forward is extra work, not counted), shots/s."""
     import numpy as np
@@ -527,8 +528,10 @@ def run_full_config(args):
                           snap_dt=3, surf_offset=0, seed=7)
     sv.imaging_sign = 1
     t0 = time.perf_counter()
-    with engine.Plan(sv, precision=32, storage="checkpoint",
-                     checkpoint_interval=c["checkpoint_interval"], **plan_kernels(args)) as p:
+    ck = dict(storage="checkpoint", checkpoint_interval=c["checkpoint_interval"])
+    if args.storage == "binomial":
+        ck = dict(storage="binomial", checkpoint_slots=args.slots)
+    with engine.Plan(sv, precision=32, **ck, **plan_kernels(args)) as p:
         p.set_model(*true)
         obs = p.forward()
         t_obs = time.perf_counter() - t0
@@ -540,9 +543,12 @@ def run_full_config(args):
         sec = time.perf_counter() - t1
         tm = p.timing()
         mem = p.device_bytes
+        kind, seg, slots, adv = p.storage
     upd = 2.0 * c["nshot"] * c["nt"] * c["nz"] * c["nx"]
     print(json.dumps({"config": args.config, "workload": {k: v for k, v in c.items()},
                       "kernels": {"family": fam, "rows_per_thread": rpt, "block_y": by},
+                      "storage": {"kind": kind, "segment_steps": seg, "slots_per_shot": slots,
+                                  "extra_segment_advances": adv},
                       "gradient_s": sec, "updates_per_s_fwd_adj": upd / sec,
                       "shots_per_s": c["nshot"] / sec, "forward_ms": tm["forward_ms"],
                       "adjoint_ms": tm["adjoint_ms"], "observed_data_s": t_obs,
@@ -577,6 +583,10 @@ def main():
                     help="--profile workload: the 301x601 bench grid or the 1001x2001 grid")
     ap.add_argument("--config", choices=["c3", "c5"], default=None,
                     help="run one gradient of a full configuration instead of the bench")
+    ap.add_argument("--storage", choices=["checkpoint", "binomial"], default="checkpoint",
+                    help="snapshot storage of the --config runs")
+    ap.add_argument("--slots", type=int, default=0,
+                    help="state slots per shot with --storage binomial (0 = the library's choice)")
     ap.add_argument("--no-uneven", action="store_true",
                     help="skip the four-survey uneven-batch leg")
     ap.add_argument("--no-large", action="store_true",

@@ -18,7 +18,7 @@ _ip = C.POINTER(C.c_int)
 PSV_OK, PSV_ERR_ARG, PSV_ERR_CFL, PSV_ERR_OOM, PSV_ERR_CUDA = 0, 1, 2, 3, 4
 PSV_ERR_UNSUPPORTED, PSV_ERR_TIMEOUT, PSV_ERR_STEP_SEARCH, PSV_ERR_IO = 5, 6, 7, 8
 STENCIL = {"reference": 0, "holberg": 1}
-STORAGE = {"auto": 0, "full": 1, "checkpoint": 2}
+STORAGE = {"auto": 0, "full": 1, "checkpoint": 2, "binomial": 3}
 
 
 class PSVError(RuntimeError):
@@ -60,7 +60,7 @@ class PsvOptions(C.Structure):
         ("precision", C.c_int), ("storage", C.c_int), ("hbm_budget_gb", C.c_double),
         ("checkpoint_interval", C.c_int), ("max_batch", C.c_int), ("use_graphs", C.c_int),
         ("block_x", C.c_int), ("block_y", C.c_int), ("rows_per_thread", C.c_int),
-        ("kernel_family", C.c_int), ("autotune", C.c_int),
+        ("kernel_family", C.c_int), ("autotune", C.c_int), ("checkpoint_slots", C.c_int),
     ]
 
 
@@ -102,6 +102,9 @@ SIGNATURES = {
     "psv_profile_kernels": (C.c_int, [C.c_void_p, C.c_int, _dp]),
     "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip]),
     "psv_plan_shape": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
+    "psv_plan_storage": (C.c_int, [C.c_void_p, _ip, _ip, _ip, C.POINTER(C.c_longlong)]),
+    "psv_checkpoint_schedule": (C.c_int, [C.c_int, C.c_int, _ip, C.c_int, _ip,
+                                          C.POINTER(C.c_longlong)]),
     "psv_multi_forward": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(_dp), C.POINTER(_dp)]),
     "psv_multi_gradient": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _dp]),
     "psv_step_length": (C.c_int, [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp, C.c_int]),

@@ -363,6 +363,14 @@ int psv_plan_autotune(psv_plan *p, int nsteps, int *family, int *rpt, int *by)
     return p->impl->autotune(nsteps, family, rpt, by);
 }
 
+int psv_plan_storage(const psv_plan *p, int *kind, int *segment_steps, int *slots,
+                     long long *advances)
+{
+    PLAN_CHECK(p);
+    p->impl->storage(kind, segment_steps, slots, advances);
+    return PSV_OK;
+}
+
 int psv_plan_shape(const psv_plan *p, int *family, int *rpt, int *by)
 {
     PLAN_CHECK(p);

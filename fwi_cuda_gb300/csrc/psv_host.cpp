@@ -4,6 +4,7 @@
 // src/h_holbergcoeff.cpp, src/h_checkfd_ssg_elastic.cpp) and readers /
 // writers of its binary files (src/h_io_PSV.cpp).  Compiled with
 // -ffp-contract=off so the profiles are bitwise equal to the reference's.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +12,7 @@
 #include <vector>
 
 #include "fwi_psv.h"
+#include "psv_checkpoint.hpp"
 #include "psv_internal.h"
 
 namespace {
@@ -267,6 +269,27 @@ extern "C" int psv_step_length(double *est_io, double L2_0, psv_trial_fn trial, 
     if (step1 == 1) est = psv_calc_opt_step(L2_test, sl);
     if (ntrials) *ntrials = n;
     *est_io = est;
+    return PSV_OK;
+}
+
+extern "C" int psv_checkpoint_schedule(int nseg, int slots, int *actions, int cap, int *nactions,
+                                       long long *advances)
+{
+    if (nseg < 1 || slots < 1) return psv::fail(PSV_ERR_ARG, "need nseg >= 1 and slots >= 1");
+    const psv::CkSchedule c = psv::ck_schedule(nseg, std::min(slots, nseg));
+    const int n = (int)(c.fwd.size() + c.bwd.size());
+    if (nactions) *nactions = n;
+    if (advances) *advances = c.advances;
+    if (!actions) return PSV_OK;
+    if (cap < n) return psv::fail(PSV_ERR_ARG, "action buffer too small");
+    int k = 0;
+    for (const auto *v : {&c.fwd, &c.bwd})
+        for (const psv::CkAction &x : *v) {
+            actions[3 * k] = x.op;
+            actions[3 * k + 1] = x.seg;
+            actions[3 * k + 2] = x.slot;
+            k++;
+        }
     return PSV_OK;
 }
 

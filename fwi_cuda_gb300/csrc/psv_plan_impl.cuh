@@ -8,6 +8,7 @@
 #include <mutex>
 #include <tuple>
 
+#include "psv_checkpoint.hpp"
 #include "psv_plan.cuh"
 
 namespace psv {
@@ -60,11 +61,16 @@ public:
     TileMaps tmap{}, tmap2{};                        // tensor maps of fld / fld2 (TMA family)
     int *h_err = nullptr;                            // pinned copy of the device error word
     std::vector<int> h_f_off;                        // host copy of the per-shot source lists
-    // Checkpointed storage: state checkpoints every K steps, a recompute
-    // state (5 field planes + CPML strips) and a segment snapshot buffer.
+    // Checkpointed storage: nck state slots at starts of K-step segments
+    // (where the schedule puts them), a working state (5 field planes + CPML
+    // strips) and a segment snapshot buffer.  nck = nseg: a state at every
+    // segment start (two-level); nck < nseg: binomial schedule.
     bool ckpt = false;
-    int K = 0, nck = 0, nslots = 0;
+    int store_kind = PSV_STORE_FULL;
+    int K = 0, nseg = 0, nck = 0, nslots = 0;
     long long ck_state = 0;  // elements of one shot's checkpointed state
+    CkSchedule sched;
+    std::vector<int> fwd_slot;  // per segment: slot the forward pass saves into, or -1
     DevMem ck, fld2, memz2, memx2;
     StepParams<T> sp{}, sp2{};
     SrcRecParams<T> qf{}, qa{}, qk{}, qr{};
@@ -164,18 +170,26 @@ public:
         // checkpointed alternative: K minimising nt/K states + K/snap_dt snapshots
         ck_state = 5 * plane + mz_shot + mx_shot;
         const double snap5 = (double)NHIST * snap_plane, sdt = g.snap_dt;
-        K = opt.checkpoint_interval > 0 ? std::min(opt.checkpoint_interval, g.nt)
-                                        : (int)std::max(1.0, std::round(std::sqrt(g.nt * (double)ck_state * sdt / snap5)));
-        K = std::min(std::max(K, 1), g.nt);
-        nck = (g.nt + K - 1) / K;
-        nslots = (K + g.snap_dt - 1) / g.snap_dt + 1;
-        const double per_ck = ((double)nck * ck_state + (double)ck_state + (double)nslots * snap5) * sizeof(T);
+        const bool binomial = opt.storage == PSV_STORE_BINOMIAL;
+        auto segments = [&](int k) {
+            K = std::min(std::max(k, 1), g.nt);
+            nseg = (g.nt + K - 1) / K;
+            nslots = (K + g.snap_dt - 1) / g.snap_dt + 1;
+        };
+        segments(opt.checkpoint_interval > 0 ? opt.checkpoint_interval
+                 : binomial ? g.snap_dt
+                            : (int)std::max(1.0, std::round(std::sqrt(g.nt * (double)ck_state * sdt / snap5))));
+        auto per_ck = [&](int slots) {
+            return ((double)slots * ck_state + (double)ck_state + (double)nslots * snap5) * sizeof(T);
+        };
         auto fit = [&](double extra) {
             int b = opt.max_batch > 0 ? std::min(opt.max_batch, nshot) : nshot;
             while (b > 1 && shared + b * (per_shot + extra) > budget) b--;
             return shared + b * (per_shot + extra) <= budget ? b : 0;
         };
-        const int b_full = fit(per_hist), b_ck = fit(per_ck);
+        const int b_full = fit(per_hist);
+        int b_ck = binomial ? 0 : fit(per_ck(nseg));
+        nck = nseg;
         if (opt.storage == PSV_STORE_FULL) {
             if (!b_full) return fail(PSV_ERR_OOM, "full snapshot history of one shot exceeds the HBM budget");
             B = b_full;
@@ -183,10 +197,32 @@ public:
             if (!b_ck) return fail(PSV_ERR_OOM, "checkpoints of one shot exceed the HBM budget");
             ckpt = true;
             B = b_ck;
-        } else {
-            if (!b_full && !b_ck) return fail(PSV_ERR_OOM, "one shot does not fit the HBM budget");
+        } else if (!binomial && (b_full || b_ck)) {
             ckpt = b_ck > b_full;
             B = ckpt ? b_ck : b_full;
+        } else {
+            // binomial: the slots asked for, else the fewest giving at most two
+            // forward repetitions (C(S + 2, 2) >= nseg), at the largest batch
+            // that holds them; with less room, one shot and every slot that fits
+            if (!binomial && opt.checkpoint_interval <= 0) segments(g.snap_dt);
+            int S = opt.checkpoint_slots > 0 ? opt.checkpoint_slots : 1;
+            if (opt.checkpoint_slots <= 0)
+                while (S < nseg && ck_reps(nseg, S) > 2) S++;
+            S = std::min(S, nseg);
+            B = fit(per_ck(S));
+            if (!B && opt.checkpoint_slots <= 0) {
+                while (S > 2 && !fit(per_ck(S))) S--;
+                B = fit(per_ck(S));
+            }
+            if (!B) return fail(PSV_ERR_OOM, "binomial checkpoints of one shot exceed the HBM budget");
+            ckpt = true;
+            nck = S;
+        }
+        if (ckpt) {
+            store_kind = nck < nseg ? PSV_STORE_BINOMIAL : PSV_STORE_CHECKPOINT;
+            sched = ck_schedule(nseg, nck);
+            fwd_slot.assign((size_t)nseg, -1);
+            for (const CkAction &x : sched.fwd) fwd_slot[(size_t)x.seg] = x.slot;
         }
         if (ckpt) hist_shot = (long long)nslots * NHIST * snap_plane;
         nbatch = (nshot + B - 1) / B;
@@ -563,15 +599,17 @@ public:
         return PSV_OK;
     }
 
-    // Copy the forward state of the batch into / out of checkpoint j.
-    int ck_copy(int j, bool save)
+    // Copy the batch's forward state between checkpoint slot j and the main
+    // state (CK_SAVE_MAIN) or the working state (CK_SAVE_WORK, CK_RESTORE).
+    int ck_copy(int j, int op)
     {
         T *c = ck.as<T>() + (size_t)j * B * ck_state;
         const size_t cp = (size_t)ck_state * sizeof(T);
-        T *f = save ? fld.as<T>() : fld2.as<T>();
-        const size_t fp = (size_t)(save ? shot_stride : 5 * plane) * sizeof(T);
-        T *mz = save ? memz.as<T>() : memz2.as<T>();
-        T *mx = save ? memx.as<T>() : memx2.as<T>();
+        const bool main = op == CK_SAVE_MAIN, save = op != CK_RESTORE;
+        T *f = main ? fld.as<T>() : fld2.as<T>();
+        const size_t fp = (size_t)(main ? shot_stride : 5 * plane) * sizeof(T);
+        T *mz = main ? memz.as<T>() : memz2.as<T>();
+        T *mx = main ? memx.as<T>() : memx2.as<T>();
         const size_t w = (size_t)5 * plane * sizeof(T);
         if (save) PSV_CU(cudaMemcpy2DAsync(c, cp, f, fp, w, B, cudaMemcpyDeviceToDevice, st));
         else PSV_CU(cudaMemcpy2DAsync(f, fp, c, cp, w, B, cudaMemcpyDeviceToDevice, st));
@@ -585,6 +623,41 @@ public:
             T *cx = c + 5 * plane + mz_shot;
             if (save) PSV_CU(cudaMemcpy2DAsync(cx, cp, mx, xw, xw, B, cudaMemcpyDeviceToDevice, st));
             else PSV_CU(cudaMemcpy2DAsync(mx, xw, cx, cp, xw, B, cudaMemcpyDeviceToDevice, st));
+        }
+        return PSV_OK;
+    }
+
+    // The adjoint pass of a checkpointed plan: the schedule's actions in
+    // order; returns the time-step launches enqueued through nk.
+    int run_schedule(long long &nk)
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        for (const CkAction &x : sched.bwd) {
+            const int a = x.seg * K, e = std::min(a + K, nt);
+            if (x.op == CK_RESTORE || x.op == CK_SAVE_WORK) {
+                PSV_TRY(ck_copy(x.slot, x.op));
+            } else if (x.op == CK_ADVANCE) {
+                for (int it = a; it < e; it++) {
+                    PSV_CU(ks(sp2, true));
+                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, -1, true));
+                }
+                nk += 2LL * (e - a);
+            } else if (x.op == CK_REVERSE) {
+                // recompute up to the segment's last snapshot step into the
+                // segment buffer, then the segment's adjoint steps
+                const int base = (a + sdt - 1) / sdt, last = (e - 1) / sdt * sdt;
+                for (int it = a; it <= last; it++) {
+                    const int slot = !(it % sdt) ? it / sdt - base : -1;
+                    PSV_CU(ks(sp2, true));
+                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, slot, true));
+                }
+                for (int it = e - 1; it >= a; it--) {
+                    const int slot = !(it % sdt) ? it / sdt - base : -1;
+                    PSV_CU(ks(sp, false));
+                    PSV_CU(kv(sp, qa, MODE_ADJ, it, slot, false));
+                }
+                nk += 2LL * (std::max(last - a + 1, 0) + e - a);
+            }
         }
         return PSV_OK;
     }
@@ -626,32 +699,16 @@ public:
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
         long long nk = (mode == MODE_ADJ ? 5 : mode == MODE_FWD ? 4 : 3);
         if (ckpt && kind == PASS_FWD_STORE) {
-            // forward keeping a state checkpoint at the start of every K-step segment
+            // forward saving the schedule's states at the starts of their segments
             for (int it = 0; it < nt; it++) {
-                if (!(it % K)) PSV_TRY(ck_copy(it / K, true));
+                if (!(it % K) && fwd_slot[(size_t)(it / K)] >= 0)
+                    PSV_TRY(ck_copy(fwd_slot[(size_t)(it / K)], CK_SAVE_MAIN));
                 PSV_CU(ks(sp, false));
                 PSV_CU(kv(sp, qf, mode, it, -1, false));
             }
             nk += 2LL * nt;
         } else if (ckpt && kind == PASS_ADJ_RES) {
-            // segments in reverse: recompute the forward from the checkpoint into
-            // the segment snapshot buffer, then the segment's adjoint steps
-            for (int j = nck - 1; j >= 0; j--) {
-                const int a = j * K, e = std::min(a + K, nt);
-                const int base = (a + sdt - 1) / sdt;
-                PSV_TRY(ck_copy(j, false));
-                for (int it = a; it < e; it++) {
-                    const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(ks(sp2, true));
-                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, slot, true));
-                }
-                for (int it = e - 1; it >= a; it--) {
-                    const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(ks(sp, false));
-                    PSV_CU(kv(sp, qa, MODE_ADJ, it, slot, false));
-                }
-            }
-            nk += 4LL * nt;
+            PSV_TRY(run_schedule(nk));
         } else {
             for (int jt = 0; jt < nt; jt++) {
                 const int it = adj ? nt - 1 - jt : jt;
@@ -1126,6 +1183,14 @@ public:
         tuned = true;
         report();
         return PSV_OK;
+    }
+
+    void storage(int *kind, int *segment_steps, int *slots, long long *advances) const override
+    {
+        if (kind) *kind = store_kind;
+        if (segment_steps) *segment_steps = ckpt ? K : 0;
+        if (slots) *slots = ckpt ? nck : 0;
+        if (advances) *advances = ckpt ? sched.advances : 0;
     }
 
     void shape(int *f, int *r, int *by) const override

@@ -25,7 +25,7 @@ FAMILIES = {1: "direct", 2: "tma", 3: "vec4"}
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
             block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
-            kernels="any") -> PsvOptions:
+            kernels="any", checkpoint_slots=0) -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -35,10 +35,24 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.use_graphs = int(bool(use_graphs))
     o.block_x, o.block_y = int(block[0]), int(block[1])
     o.checkpoint_interval = int(checkpoint_interval)
+    o.checkpoint_slots = int(checkpoint_slots)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
     o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3}[kernels]
     return o
+
+
+def checkpoint_schedule(nseg, slots):
+    """Griewank's binomial schedule for nseg segments and `slots` state slots
+    (host only): (actions, advances), actions an (n, 3) array of
+    (op, segment, slot) -- op 1 forward-pass save, 2 restore, 3 advance,
+    4 save the working state, 5 recompute + reverse a segment."""
+    n, adv = C.c_int(), C.c_longlong()
+    check(_lib.lib().psv_checkpoint_schedule(int(nseg), int(slots), None, 0, C.byref(n), C.byref(adv)))
+    a = np.zeros((max(n.value, 1), 3), np.int32)
+    check(_lib.lib().psv_checkpoint_schedule(int(nseg), int(slots), iptr(a), n.value, C.byref(n),
+                                             C.byref(adv)))
+    return a[:n.value], adv.value
 
 
 class Plan:
@@ -178,6 +192,17 @@ class Plan:
         f, r, b = C.c_int(), C.c_int(), C.c_int()
         check(_lib.lib().psv_plan_shape(self.h, C.byref(f), C.byref(r), C.byref(b)))
         return FAMILIES[f.value], r.value, b.value
+
+    @property
+    def storage(self):
+        """(storage, segment_steps, slots, advances): "full", "checkpoint" or
+        "binomial"; steps per checkpoint segment and state slots per shot;
+        segment advances the adjoint pass recomputes beyond one
+        recomputation of every segment."""
+        k, K, S, a = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        check(_lib.lib().psv_plan_storage(self.h, C.byref(k), C.byref(K), C.byref(S), C.byref(a)))
+        name = {v: n for n, v in _lib.STORAGE.items()}[k.value]
+        return name, K.value, S.value, a.value
 
     def profile_kernels(self, nsteps=100):
         ms = np.zeros(6)

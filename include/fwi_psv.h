@@ -43,9 +43,12 @@ typedef enum {
 #define PSV_STENCIL_REFERENCE 0 /* reference: 2-point difference x hc[1], pad fdorder/2 */
 #define PSV_STENCIL_HOLBERG 1   /* full 2N-point staggered Holberg stencil, N = fdorder/2 */
 
-#define PSV_STORE_AUTO 0        /* full history when it fits the budget, else checkpoints */
+#define PSV_STORE_AUTO 0        /* full history when it fits the budget, else CHECKPOINT,
+                                   else BINOMIAL */
 #define PSV_STORE_FULL 1        /* every snapshot kept in HBM (the reference's accu_*) */
-#define PSV_STORE_CHECKPOINT 2  /* checkpoints + recomputation of the forward */
+#define PSV_STORE_CHECKPOINT 2  /* a state at every segment start + one recomputed forward */
+#define PSV_STORE_BINOMIAL 3    /* fewer state slots than segments, placed by Griewank's
+                                   binomial schedule (more recomputation, less memory) */
 
 /* Time-step kernel families (psv_options.kernel_family). */
 #define PSV_KERNELS_DIRECT 1    /* per-thread loads of the stencil neighbours */
@@ -124,7 +127,8 @@ typedef struct psv_options {
     int precision;              /* 32 (default) or 64 */
     int storage;                /* PSV_STORE_* */
     double hbm_budget_gb;       /* device memory the plan may use; 0 = 180 */
-    int checkpoint_interval;    /* CHECKPOINT storage: steps per segment, 0 = auto */
+    int checkpoint_interval;    /* CHECKPOINT / BINOMIAL storage: steps per segment, 0 = auto
+                                   (balanced for CHECKPOINT, snap_dt for BINOMIAL) */
     int max_batch;              /* shots per launch; 0 = all shots of the survey */
     int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
     int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
@@ -137,6 +141,9 @@ typedef struct psv_options {
     int autotune;               /* 1 (default): time the tile-shape candidates on the first
                                    time loop and keep the fastest (psv_plan_autotune);
                                    0: use block_y / rows_per_thread as given */
+    int checkpoint_slots;       /* BINOMIAL storage: state slots per shot (segment 0's
+                                   included); 0 = the fewest with at most two forward
+                                   repetitions, fewer if the budget holds fewer */
 } psv_options;
 
 void psv_options_default(psv_options *opt);
@@ -295,6 +302,23 @@ int psv_plan_autotune(psv_plan *plan, int nsteps, int *kernel_family, int *rows_
 /* The time-step kernels the plan launches now: family (PSV_KERNELS_*), rows
  * per thread and block height (any pointer may be NULL). */
 int psv_plan_shape(const psv_plan *plan, int *kernel_family, int *rows_per_thread, int *block_y);
+/* The plan's snapshot storage: PSV_STORE_FULL, _CHECKPOINT or _BINOMIAL
+ * (never AUTO), steps per segment and state slots per shot (0 for FULL),
+ * and the segment advances the adjoint pass recomputes beyond the one
+ * recomputation of each segment (0 unless BINOMIAL).  Any pointer may be
+ * NULL.  Replaces the accu_* allocation in the reference's
+ * simulate_fwi_PSV (src/cpu/n_simulate_PSV.cpp). */
+int psv_plan_storage(const psv_plan *plan, int *storage, int *segment_steps, int *slots,
+                     long long *advances);
+/* Griewank's binomial checkpoint schedule for nseg segments and `slots`
+ * state slots (host only, no device): writes up to `cap` actions as
+ * (op, segment, slot) triples into `actions` -- first the forward pass's
+ * saves (op 1), then the adjoint pass (2 restore, 3 advance, 4 save the
+ * working state, 5 recompute + reverse a segment) -- and their count into
+ * *nactions, and the advances into *advances.  PSV_ERR_ARG if cap is too
+ * small (the counts are still written). */
+int psv_checkpoint_schedule(int nseg, int slots, int *actions, int cap, int *nactions,
+                            long long *advances);
 
 /* The CUDA stream every call of this plan runs on (a cudaStream_t), for
  * callers that time or order work against it. */

@@ -94,18 +94,19 @@ def test_tiled_families_against_oracle(gpu, orc, kw, fam, rpt):
 
 
 @pytest.mark.parametrize("fam", ["tma", "vec4"])
-def test_tiled_families_checkpointed_equals_full(gpu, orc, fam):
+def test_tiled_families_checkpointed_equal_full(gpu, orc, fam):
     sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, snap_dt=3)
     uz, ux = orc.simulate_fwd(sv, *true)
     out = []
-    for storage in ("full", "checkpoint"):
+    for storage, slots in (("full", 0), ("checkpoint", 0), ("binomial", 3)):
         with engine.Plan(sv, precision=32, kernels=fam, rows_per_thread=2,
-                         storage=storage, checkpoint_interval=40) as p:
-            assert p.shape[0] == fam
+                         storage=storage, checkpoint_interval=40, checkpoint_slots=slots) as p:
+            assert p.shape[0] == fam and p.storage[0] == storage
             p.set_model(*init)
             p.set_observed(uz, ux)
             out.append(p.gradient())
-    (La, ga), (Lb, gb) = out
-    assert La == Lb
-    for a, b in zip(ga, gb):
-        assert np.array_equal(a, b)
+    (La, ga), *rest = out
+    for Lb, gb in rest:
+        assert La == Lb
+        for a, b in zip(ga, gb):
+            assert np.array_equal(a, b)

@@ -113,6 +113,69 @@ def test_checkpointed_gradient_bitwise_equals_full_storage(gpu, orc, precision, 
             assert np.array_equal(x[k], y[k]), k
 
 
+@pytest.mark.parametrize("precision,interval,slots", [(32, 0, 1), (32, 0, 3), (32, 7, 2),
+                                                      (64, 0, 4), (32, 11, 0)])
+def test_binomial_checkpoints_bitwise_equal_full_storage(gpu, orc, precision, interval, slots):
+    # fewer state slots than segments: segments are reached again by advancing
+    # from earlier states (Griewank's schedule); still deterministic, bound 0
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=2, nt=301,
+                                    snap_dt=2)
+    res = {}
+    for storage in ("full", "binomial"):
+        with engine.Plan(sv, precision=precision, storage=storage, checkpoint_interval=interval,
+                         checkpoint_slots=slots) as p:
+            kind, K, S, adv = p.storage
+            assert kind == storage
+            if storage == "binomial":
+                nseg = -(-sv.nt // K)
+                assert K == (interval or sv.snap_dt) and S < nseg and adv > 0
+                assert S == slots or slots == 0
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            res[storage] = (p.gradient(), [p.shot_gradient(s) for s in range(sv.nshot)])
+    (L2a, ga), sa = res["full"]
+    (L2b, gb), sb = res["binomial"]
+    assert L2a == L2b
+    for a, b in zip(ga, gb):
+        assert np.array_equal(a, b)
+    for x, y in zip(sa, sb):
+        for k in ("grad_lam", "grad_mu", "grad_rho", "We", "We_adj"):
+            assert np.array_equal(x[k], y[k]), k
+
+
+def test_auto_storage_falls_back_to_binomial(gpu, orc):
+    # a budget below what the two-level scheme needs for one shot
+    sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=1, nt=400)
+    with engine.Plan(sv, storage="checkpoint", max_batch=1) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        p.gradient(fetch=False)  # checkpoints are allocated by the first gradient
+        need = p.device_bytes
+    kinds = []
+    for f in (0.9, 0.8, 0.7, 0.6, 0.5, 0.4):
+        try:
+            with engine.Plan(sv, storage="auto", max_batch=1, hbm_budget_gb=f * need / 1e9) as p:
+                kinds.append(p.storage[0])
+                if kinds[-1] != "binomial":
+                    continue
+                p.set_model(*init)
+                p.set_observed(uz, ux)
+                L2, g = p.gradient()
+                assert p.device_bytes < need
+            break
+        except Exception as e:  # too small for any storage
+            kinds.append(str(e))
+            break
+    assert "binomial" in kinds, kinds
+    with engine.Plan(sv, storage="full") as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L2f, gf = p.gradient()
+    assert L2 == L2f
+    for a, b in zip(g, gf):
+        assert np.array_equal(a, b)
+
+
 def test_checkpoint_storage_uses_less_memory(gpu, orc):
     sv, true, init, uz, ux = _setup(orc, fdorder=4, stencil="holberg", nshot=2, nt=600)
     mem = {}
