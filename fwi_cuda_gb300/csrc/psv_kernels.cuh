@@ -19,10 +19,18 @@ namespace psv {
 
 // Planes of one shot's wavefield block [NFIELD][nz][pitch].
 enum { F_VZ = 0, F_VX, F_SZZ, F_SZX, F_SXX, F_UZ, F_UX, F_WE, F_WEA, NFIELD };
+// FP32 plans also hold a second copy of vz vx szz szx sxx at planes
+// NFIELD .. NFIELD + 4 for the fused time step, which reads one copy and
+// writes the other (ping-pong by step parity).
+constexpr int NFIELD_PP = NFIELD + 5;
 // z-strip CPML memories (rows outside [pz0, pz1)): mem_vz_z, mem_vx_z, mem_szz_z, mem_szx_z.
 enum { MZ_VZ = 0, MZ_VX, MZ_SZZ, MZ_SZX, NMZ };
 // x-strip CPML memories (columns outside [px0, px1)): mem_vz_x, mem_vx_x, mem_szx_x, mem_sxx_x.
 enum { MX_VZ = 0, MX_VX, MX_SZX, MX_SXX, NMX };
+// FP32 plans: second copies of the memories the stress update reads at
+// halo points (mem_vz_z, mem_vx_z at planes NMZ, NMZ + 1; mem_vz_x, mem_vx_x
+// at NMX, NMX + 1), ping-ponged by the fused time step.
+constexpr int NMZ_PP = NMZ + 2, NMX_PP = NMX + 2;
 // Snapshot planes of one stored step: accu_szz, accu_szx, accu_sxx, accu_vz, accu_vx.
 enum { H_SZZ = 0, H_SZX, H_SXX, H_VZ, H_VX, NHIST };
 // Velocity-kernel modes: forward with the energy We; forward without it
@@ -66,6 +74,7 @@ struct StepParams {
     const int *ctl;            // device [2]: global index of batch shot 0, shots in this batch
     int *err;                  // device error word (nonzero: a bounded wait gave up)
     int nbatch;                // shots per launch (grid extent in shots)
+    int pp_planes;             // planes from the first to the second vz..sxx copy (0: none)
 };
 
 // Block coordinates of the grid-stepping kernels: blockIdx.z = shot of the

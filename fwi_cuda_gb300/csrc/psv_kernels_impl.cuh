@@ -242,12 +242,13 @@ __device__ __forceinline__ void image_apply(const StepParams<T> &p, int bz, cons
 // update_v2 (src/cpu/n_kernel_lib_PSV.cpp:243-270) of interior point i from
 // its old velocities, plus the displacement integration (adjoint and the
 // drop-in forward) and the energy sum We / We_adj from the old u / We
-// values; stores and returns the new values.
+// values; stores and returns the new values.  The new velocities go to the
+// planes of `fv` when given (the fused step's write copy), else of f.
 template <typename T, int MODE>
 __device__ __forceinline__ void velocity_finish(const StepParams<T> &p, T *f, long long i, T vzo,
                                                 T vxo, T uzo, T uxo, T weo, T crz, T crx,
                                                 T szz_z, T szx_z, T szx_x, T sxx_x, T &vzn,
-                                                T &vxn, T &uzn, T &uxn)
+                                                T &vxn, T &uzn, T &uxn, T *fv = nullptr)
 {
     if (MODE == MODE_ADJ || MODE == MODE_FWD_U) {
         uzn = uzo + p.dt * vzo;
@@ -257,8 +258,9 @@ __device__ __forceinline__ void velocity_finish(const StepParams<T> &p, T *f, lo
     }
     vzn = vzo + crz * (szx_x + szz_z);
     vxn = vxo + crx * (sxx_x + szx_z);
-    f[F_VZ * p.plane + i] = vzn;
-    f[F_VX * p.plane + i] = vxn;
+    T *vb = fv ? fv : f;
+    vb[F_VZ * p.plane + i] = vzn;
+    vb[F_VX * p.plane + i] = vxn;
     if (MODE != MODE_FWD_NOWE)
         f[(MODE == MODE_ADJ ? F_WEA : F_WE) * p.plane + i] = weo + (vxn * vxn + vzn * vzn);
 }
@@ -296,13 +298,14 @@ __device__ __forceinline__ TileSR tile_srcrec(const StepParams<T> &p, const SrcR
 // with the tile's index entries `e`.
 template <typename T, int MODE>
 __device__ __forceinline__ void srcrec_apply(const StepParams<T> &p, const SrcRecParams<T> &q,
-                                             int it, int slot, int bz, TileSR e, int tid, int nth)
+                                             int it, int slot, int bz, TileSR e, int tid, int nth,
+                                             T *fbase = nullptr)
 {
     const int k0 = e.k0, k1 = e.k1;
     const bool recs = e.r0 < e.r1;
     if (k0 == k1 && !recs) return;  // uniform over the block
     const int shot = p.ctl[0] + bz;
-    T *f = p.fld + (long long)bz * p.shot_stride;
+    T *f = (fbase ? fbase : p.fld) + (long long)bz * p.shot_stride;  // planes holding the new v
     T *vz = f + F_VZ * p.plane;
     T *vx = f + F_VX * p.plane;
     const long long sp = p.snap_plane;

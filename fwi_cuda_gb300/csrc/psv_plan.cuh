@@ -43,6 +43,13 @@ cudaError_t launch_stress_v4(const StepParams<float> &p, int ns, int rpt, int by
 cudaError_t launch_velocity_v4(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
                                int mode, int it, int slot, int rpt, int by, int nbatch,
                                cudaStream_t st);
+// Fused time step (FP32, psv_fused.cu): one launch per step over tiles of
+// 64 columns x tz rows (tz 16 or 32), reading field copy `par` and writing
+// copy 1 - par.  fused_supported: the surfaces it handles (top only).
+bool fused_supported(int ns, int tz, int st, int sb, int sl, int sr, int nz1);
+cudaError_t launch_step_fused(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
+                              int mode, int it, int slot, int par, int tz, int nbatch,
+                              cudaStream_t st);
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
 cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,

@@ -132,10 +132,10 @@ public:
         const psv_grid &g = sv.g;
         const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
         const int al = 128 / (int)sizeof(T);
-        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_VEC4)
-            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2 or 3");
+        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_FUSED)
+            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2, 3 or 4");
         if (opt.kernel_family >= PSV_KERNELS_TMA && sizeof(T) != 4)
-            return fail(PSV_ERR_UNSUPPORTED, "TMA and VEC4 kernels are FP32 only");
+            return fail(PSV_ERR_UNSUPPORTED, "TMA, VEC4 and FUSED kernels are FP32 only");
         if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
         if (opt.block_y > 0 || opt.rows_per_thread) opt.autotune = 0;  // explicit shape wins
         if (opt.kernel_family == PSV_KERNELS_TMA) {
@@ -145,18 +145,24 @@ public:
             fam = PSV_KERNELS_VEC4;
             rpt = v4_rpt(opt.rows_per_thread ? opt.rows_per_thread : 1);
             if (opt.block_y <= 0) blk = dim3(32, 4, 1);
+        } else if (opt.kernel_family == PSV_KERNELS_FUSED) {
+            fam = PSV_KERNELS_FUSED;
+            rpt = fused_tz(opt.rows_per_thread ? opt.rows_per_thread : 32);
+            if (!fused_ok(rpt))
+                return fail(PSV_ERR_UNSUPPORTED, "fused time step: only a top free surface, within "
+                                                 "the first tile row");
         } else {
             rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
             if (opt.block_y <= 0) blk = dim3(32, 4, 1);
         }
         pitch = round_up(nx, al);
         plane = (long long)nz * pitch;
-        shot_stride = NFIELD * plane;
+        shot_stride = (long long)nfield() * plane;
         nzs = g.pml_z ? sv.pz0 + (nz - sv.pz1) : 0;
         nxs = g.pml_x ? sv.px0 + (nx - sv.px1) : 0;
         mx_pitch = nxs ? round_up(nxs, al) : 0;
-        mz_shot = (long long)NMZ * nzs * pitch;
-        mx_shot = (long long)NMX * nz * mx_pitch;
+        mz_shot = (long long)(sizeof(T) == 4 ? NMZ_PP : NMZ) * nzs * pitch;
+        mx_shot = (long long)(sizeof(T) == 4 ? NMX_PP : NMX) * nz * mx_pitch;
         snx_pitch = round_up(sv.snx, al);
         const long long snap_plane = (long long)sv.snz * snx_pitch;
         hist_shot = (long long)sv.snt * NHIST * snap_plane;
@@ -273,6 +279,19 @@ public:
     }
 
     static int tma_rpt(int r) { return (r == 2 || r == 4 || r == 8) ? r : 4; }
+    static int fused_tz(int r) { return (r == 16 || r == 32) ? r : 32; }
+    bool fused_ok(int tz) const
+    {
+        return sizeof(T) == 4 && fused_supported(sv.ns, tz, sv.st, sv.sb, sv.sl, sv.sr, sv.nz1);
+    }
+    // Field planes per shot: FP32 plans hold the second vz..sxx copy of the
+    // fused step; the working (recompute) state has 5 planes, 10 in FP32.
+    static constexpr int nfield() { return sizeof(T) == 4 ? NFIELD_PP : NFIELD; }
+    static constexpr int nwork() { return sizeof(T) == 4 ? 10 : 5; }
+    bool fused() const { return fam == PSV_KERNELS_FUSED; }
+    // Copy of v and sigma a step reads: step k of a pass reads copy k & 1
+    // (the fused family ping-pongs; the others update in place, copy 0).
+    int par(int k) const { return fused() ? (k & 1) : 0; }
     static int v4_rpt(int r) { return (r == 1 || r == 2 || r == 4) ? r : 1; }
 
     // Tensor maps of the field blocks for the TMA family (rebuilt when the
@@ -282,10 +301,10 @@ public:
         if constexpr (sizeof(T) == 4) {
             if (fam != PSV_KERNELS_TMA) return PSV_OK;
             const psv_grid &g = sv.g;
-            PSV_TRY(encode_tile_maps(&tmap, fld.as<float>(), (int)(B * NFIELD), coef.as<float>(),
+            PSV_TRY(encode_tile_maps(&tmap, fld.as<float>(), (int)(B * nfield()), coef.as<float>(),
                                      g.nx, g.nz, pitch, plane, sv.ns, rpt));
             if (fld2.p)
-                PSV_TRY(encode_tile_maps(&tmap2, fld2.as<float>(), B * 5, coef.as<float>(), g.nx,
+                PSV_TRY(encode_tile_maps(&tmap2, fld2.as<float>(), B * nwork(), coef.as<float>(), g.nx,
                                          g.nz, pitch, plane, sv.ns, rpt));
         }
         return PSV_OK;
@@ -316,6 +335,19 @@ public:
         (void)second;
         return launch_velocity<T>(s, q, sv.ns, mode, it, slot, rpt, blk, B, st);
     }
+
+    // One time step: the family's stress and velocity launches, or the fused
+    // launch reading copy `pr` of v and sigma and writing the other.
+    cudaError_t step(const StepParams<T> &s, const SrcRecParams<T> &q, int mode, int it, int slot,
+                     bool second, int pr)
+    {
+        if constexpr (sizeof(T) == 4)
+            if (fused()) return launch_step_fused(s, q, sv.ns, mode, it, slot, pr, rpt, B, st);
+        cudaError_t e = ks(s, second);
+        if (e != cudaSuccess) return e;
+        return kv(s, q, mode, it, slot, second);
+    }
+    long long lps() const { return fused() ? 1 : 2; }  // launches per step
 
     // Wait for the stream, then fail if a time-step kernel gave up a bounded
     // wait (device error word).
@@ -407,13 +439,13 @@ public:
 
     // Sources and receivers bucketed by the velocity kernel's tiles (direct
     // family: 32 columns x blk.y * |rpt| rows; TMA: 64 x 4 rpt; VEC4: 128 x
-    // blk.y * rpt), so each block finds its own.
+    // blk.y * rpt; FUSED: 64 x rpt), so each block finds its own.
     int build_tile_index()
     {
         const int nshot = sv.s.nshot, nrec = sv.s.nrec;
         const bool tma = fam == PSV_KERNELS_TMA, v4 = fam == PSV_KERNELS_VEC4;
-        const int tw = tma ? 64 : v4 ? 128 : 32;
-        const int tz = tma ? 4 * rpt : (int)blk.y * (rpt < 0 ? -rpt : rpt);
+        const int tw = tma || fused() ? 64 : v4 ? 128 : 32;
+        const int tz = tma ? 4 * rpt : fused() ? rpt : (int)blk.y * (rpt < 0 ? -rpt : rpt);
         const int ntx = (sv.g.nx + tw - 1) / tw, ntz = (sv.g.nz + tz - 1) / tz;
         const int nt_ = ntx * ntz;
         auto tile_of = [&](int z, int x) { return (z / tz) * ntx + x / tw; };
@@ -575,8 +607,10 @@ public:
         qa.src_kind = 1;
         qr = qf;  // recomputed forward: sources and snapshot fix-ups, no recording
         qr.rtf_z = qr.rtf_x = nullptr;
-        sp2 = p;  // recompute state: 5 planes per shot and its own CPML strips
-        sp2.shot_stride = 5 * plane;
+        sp.pp_planes = sizeof(T) == 4 ? NFIELD : 0;
+        sp2 = sp;  // recompute state: 5 planes per shot (10 in FP32) and its own CPML strips
+        sp2.shot_stride = nwork() * plane;
+        sp2.pp_planes = sizeof(T) == 4 ? 5 : 0;
     }
 
     int ensure_hist()
@@ -586,9 +620,11 @@ public:
         sp.hist = hist.as<T>();
         if (ckpt) {
             PSV_TRY(ck.alloc((size_t)nck * B * ck_state * sizeof(T), total));
-            PSV_TRY(fld2.alloc((size_t)B * 5 * plane * sizeof(T), total));
+            PSV_TRY(fld2.alloc((size_t)B * nwork() * plane * sizeof(T), total));
             PSV_TRY(memz2.alloc((size_t)B * mz_shot * sizeof(T), total));
             PSV_TRY(memx2.alloc((size_t)B * mx_shot * sizeof(T), total));
+            // padding columns are read by the fused step's staging copies
+            PSV_CU(cudaMemsetAsync(fld2.p, 0, fld2.bytes, st));
             sp2.fld = fld2.as<T>();
             sp2.memz = memz2.as<T>();
             sp2.memx = memx2.as<T>();
@@ -600,14 +636,17 @@ public:
     }
 
     // Copy the batch's forward state between checkpoint slot j and the main
-    // state (CK_SAVE_MAIN) or the working state (CK_SAVE_WORK, CK_RESTORE).
-    int ck_copy(int j, int op)
+    // state (CK_SAVE_MAIN) or the working state (CK_SAVE_WORK, CK_RESTORE),
+    // taking v and sigma from / to copy pr.  The CPML strips are copied
+    // whole (both copies of the ping-ponged memories).
+    int ck_copy(int j, int op, int pr)
     {
         T *c = ck.as<T>() + (size_t)j * B * ck_state;
         const size_t cp = (size_t)ck_state * sizeof(T);
         const bool main = op == CK_SAVE_MAIN, save = op != CK_RESTORE;
-        T *f = main ? fld.as<T>() : fld2.as<T>();
-        const size_t fp = (size_t)(main ? shot_stride : 5 * plane) * sizeof(T);
+        T *f = main ? fld.as<T>() + (size_t)pr * sp.pp_planes * plane
+                    : fld2.as<T>() + (size_t)pr * sp2.pp_planes * plane;
+        const size_t fp = (size_t)(main ? shot_stride : nwork() * plane) * sizeof(T);
         T *mz = main ? memz.as<T>() : memz2.as<T>();
         T *mx = main ? memx.as<T>() : memx2.as<T>();
         const size_t w = (size_t)5 * plane * sizeof(T);
@@ -634,29 +673,27 @@ public:
         const int nt = sv.g.nt, sdt = sv.g.snap_dt;
         for (const CkAction &x : sched.bwd) {
             const int a = x.seg * K, e = std::min(a + K, nt);
+            // the working state of forward step it is copy par(it) (as in the
+            // forward pass); adjoint step it is step nt - 1 - it of its pass
             if (x.op == CK_RESTORE || x.op == CK_SAVE_WORK) {
-                PSV_TRY(ck_copy(x.slot, x.op));
+                PSV_TRY(ck_copy(x.slot, x.op, par(a)));
             } else if (x.op == CK_ADVANCE) {
-                for (int it = a; it < e; it++) {
-                    PSV_CU(ks(sp2, true));
-                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, -1, true));
-                }
-                nk += 2LL * (e - a);
+                for (int it = a; it < e; it++)
+                    PSV_CU(step(sp2, qr, MODE_FWD_NOWE, it, -1, true, par(it)));
+                nk += lps() * (e - a);
             } else if (x.op == CK_REVERSE) {
                 // recompute up to the segment's last snapshot step into the
                 // segment buffer, then the segment's adjoint steps
                 const int base = (a + sdt - 1) / sdt, last = (e - 1) / sdt * sdt;
                 for (int it = a; it <= last; it++) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(ks(sp2, true));
-                    PSV_CU(kv(sp2, qr, MODE_FWD_NOWE, it, slot, true));
+                    PSV_CU(step(sp2, qr, MODE_FWD_NOWE, it, slot, true, par(it)));
                 }
                 for (int it = e - 1; it >= a; it--) {
                     const int slot = !(it % sdt) ? it / sdt - base : -1;
-                    PSV_CU(ks(sp, false));
-                    PSV_CU(kv(sp, qa, MODE_ADJ, it, slot, false));
+                    PSV_CU(step(sp, qa, MODE_ADJ, it, slot, false, par(nt - 1 - it)));
                 }
-                nk += 2LL * (std::max(last - a + 1, 0) + e - a);
+                nk += lps() * (std::max(last - a + 1, 0) + e - a);
             }
         }
         return PSV_OK;
@@ -684,6 +721,8 @@ public:
         T *f = fld.as<T>();
         const long long n0 = nlaunch;
         // reset_sv2 / reset_PML_memory2 / reset_grad_shot2 (n_kernel_PSV.cpp:74-88)
+        if (fused())  // the second copy of v and sigma
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, (long long)NFIELD * plane, 5 * plane, B, st));
         if (mode == MODE_ADJ) {
             PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 7 * plane, B, st));
             PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WEA * plane, plane, B, st));
@@ -702,21 +741,19 @@ public:
             // forward saving the schedule's states at the starts of their segments
             for (int it = 0; it < nt; it++) {
                 if (!(it % K) && fwd_slot[(size_t)(it / K)] >= 0)
-                    PSV_TRY(ck_copy(fwd_slot[(size_t)(it / K)], CK_SAVE_MAIN));
-                PSV_CU(ks(sp, false));
-                PSV_CU(kv(sp, qf, mode, it, -1, false));
+                    PSV_TRY(ck_copy(fwd_slot[(size_t)(it / K)], CK_SAVE_MAIN, par(it)));
+                PSV_CU(step(sp, qf, mode, it, -1, false, par(it)));
             }
-            nk += 2LL * nt;
+            nk += lps() * nt;
         } else if (ckpt && kind == PASS_ADJ_RES) {
             PSV_TRY(run_schedule(nk));
         } else {
             for (int jt = 0; jt < nt; jt++) {
                 const int it = adj ? nt - 1 - jt : jt;
                 const bool snap = !(it % sdt);
-                PSV_CU(ks(sp, false));
-                PSV_CU(kv(sp, q, mode, it, (snap && (store || adj)) ? it / sdt : -1, false));
+                PSV_CU(step(sp, q, mode, it, (snap && (store || adj)) ? it / sdt : -1, false, par(jt)));
             }
-            nk += 2LL * nt;
+            nk += lps() * nt;
         }
         nlaunch = n0 + nk;
         return PSV_OK;
@@ -1116,8 +1153,13 @@ public:
     int set_shape(int f, int r, int by)
     {
         if (f >= PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
-        r = f == PSV_KERNELS_TMA ? tma_rpt(r) : f == PSV_KERNELS_VEC4 ? v4_rpt(r) : rpt_ok<T>(r);
+        if (f == PSV_KERNELS_FUSED && !fused_ok(fused_tz(r))) f = PSV_KERNELS_DIRECT;
+        r = f == PSV_KERNELS_TMA     ? tma_rpt(r)
+            : f == PSV_KERNELS_VEC4  ? v4_rpt(r)
+            : f == PSV_KERNELS_FUSED ? fused_tz(r)
+                                     : rpt_ok<T>(r);
         if (f == PSV_KERNELS_TMA) by = 4;
+        if (f == PSV_KERNELS_FUSED) by = (int)blk.y;  // unused
         if (f == fam && r == rpt && (int)blk.y == by) return PSV_OK;
         fam = f;
         rpt = r;
@@ -1166,6 +1208,9 @@ public:
         if (sizeof(T) == 4 && (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_VEC4))
             for (int r : {1, 2, 4})
                 for (int by : {2, 4, 8}) cand.emplace_back(PSV_KERNELS_VEC4, r, by);
+        if (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_FUSED)
+            for (int tz : {16, 32})
+                if (fused_ok(tz)) cand.emplace_back(PSV_KERNELS_FUSED, tz, (int)blk.y);
         double best = 1e30;
         std::tuple<int, int, int> pick{fam, rpt, (int)blk.y};
         for (auto &c : cand) {
@@ -1197,7 +1242,7 @@ public:
     {
         if (f) *f = fam;
         if (r) *r = rpt;
-        if (by) *by = fam == PSV_KERNELS_TMA ? 4 : (int)blk.y;
+        if (by) *by = fam == PSV_KERNELS_TMA ? 4 : fused() ? 0 : (int)blk.y;
     }
 
     int prepare() override
@@ -1228,7 +1273,7 @@ public:
         for (auto &x : e) PSV_CU(cudaEventCreate(&x));
         const int nt = sv.g.nt, sdt = sv.g.snap_dt;
         T *f = fld.as<T>();
-        PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, (long long)NFIELD * plane, B, st));
+        PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, shot_stride, B, st));
         PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
         int rc = PSV_OK;
@@ -1239,15 +1284,17 @@ public:
                 const int it = adj ? nt - 1 - j : j;
                 const int slot = !(it % sdt) ? (it / sdt) % (ckpt ? nslots : sv.snt) : -1;
                 cudaEvent_t *E = &e[(size_t)(pass * nsteps + j) * 4];
+                // fused family: the whole step is timed in the velocity slot
                 cudaEventRecord(E[0], st);
-                cudaError_t c = ks(sp, false);
+                cudaError_t c = fused() ? cudaSuccess : ks(sp, false);
                 cudaEventRecord(E[1], st);
                 if (c == cudaSuccess)
-                    c = kv(sp, q, adj ? MODE_ADJ : MODE_FWD, it, slot, false);
+                    c = fused() ? step(sp, q, adj ? MODE_ADJ : MODE_FWD, it, slot, false, par(j))
+                                : kv(sp, q, adj ? MODE_ADJ : MODE_FWD, it, slot, false);
                 cudaEventRecord(E[2], st);
                 cudaEventRecord(E[3], st);
                 if (c != cudaSuccess) { rc = fail(PSV_ERR_CUDA, cudaGetErrorString(c)); break; }
-                nlaunch += 2;
+                nlaunch += lps();
             }
         }
         if (rc == PSV_OK) rc = sync_check();
@@ -1317,7 +1364,11 @@ public:
         // wavefields: vz vx uz ux szz szx sxx We
         std::vector<T> pl((size_t)shot_stride);
         PSV_CU(cudaMemcpy(pl.data(), fld.p, pl.size() * sizeof(T), cudaMemcpyDeviceToHost));
-        const int fmap[8] = {F_VZ, F_VX, F_UZ, F_UX, F_SZZ, F_SZX, F_SXX, grad_ ? F_WEA : F_WE};
+        // the pass's last step wrote copy par(nt) of v, sigma and the
+        // stress-side CPML memories
+        const int fp = par(g.nt), vo = fp * sp.pp_planes;
+        const int fmap[8] = {F_VZ + vo, F_VX + vo, F_UZ, F_UX, F_SZZ + vo, F_SZX + vo, F_SXX + vo,
+                             grad_ ? F_WEA : F_WE};
         for (int k = 0; k < 8; k++)
             if (fields_out[k])
                 for (int iz = 0; iz < nz; iz++)
@@ -1335,11 +1386,13 @@ public:
                 for (int ix = 0; ix < nx; ix++) {
                     if (k < 4 && nzs && (iz < sv.pz0 || iz >= sv.pz1)) {
                         const int r = iz < sv.pz0 ? iz : iz - sv.pz1 + sv.pz0;
-                        mem_out[k][(size_t)iz * nx + ix] = (double)mz[(size_t)k * nzs * pitch + (size_t)r * pitch + ix] * un;
+                        const int pl = k + (k == MZ_VZ || k == MZ_VX ? fp * NMZ : 0);
+                        mem_out[k][(size_t)iz * nx + ix] = (double)mz[(size_t)pl * nzs * pitch + (size_t)r * pitch + ix] * un;
                     } else if (k >= 4 && nxs && (ix < sv.px0 || ix >= sv.px1)) {
                         const int c = ix < sv.px0 ? ix : ix - sv.px1 + sv.px0;
+                        const int pl = (k - 4) + (k - 4 == MX_VZ || k - 4 == MX_VX ? fp * NMX : 0);
                         mem_out[k][(size_t)iz * nx + ix] =
-                            (double)mxv[(size_t)(k - 4) * nz * mx_pitch + (size_t)iz * mx_pitch + c] * un;
+                            (double)mxv[(size_t)pl * nz * mx_pitch + (size_t)iz * mx_pitch + c] * un;
                     }
                 }
         }

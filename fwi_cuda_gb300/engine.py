@@ -20,7 +20,7 @@ from . import _lib
 from ._lib import PsvOptions, check, dptr, f64, i32, iptr
 
 
-FAMILIES = {1: "direct", 2: "tma", 3: "vec4"}
+FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused"}
 
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
@@ -38,7 +38,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.checkpoint_slots = int(checkpoint_slots)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
-    o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3}[kernels]
+    o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4}[kernels]
     return o
 
 

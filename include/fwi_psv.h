@@ -54,6 +54,8 @@ typedef enum {
 #define PSV_KERNELS_DIRECT 1    /* per-thread loads of the stencil neighbours */
 #define PSV_KERNELS_TMA 2       /* tiles staged in shared memory by TMA tensor copies (FP32) */
 #define PSV_KERNELS_VEC4 3      /* four columns per thread, 128-bit loads and stores (FP32) */
+#define PSV_KERNELS_FUSED 4     /* one launch per time step: stress of a tile and its halo,
+                                   then its velocities, from shared memory (FP32) */
 
 const char *psv_error_string(int status);
 /* Message of the last failing call on this host thread. */
@@ -134,10 +136,10 @@ typedef struct psv_options {
     int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
     int rows_per_thread;        /* rows each thread marches: direct family 1, 2, 4 (negative:
                                    warp-shuffle variant); TMA family 2, 4, 8; VEC4 family
-                                   1, 2, 4; 0 = default */
+                                   1, 2, 4; FUSED family: tile rows 16 or 32; 0 = default */
     int kernel_family;          /* time-step kernels: 0 = any (the autotuner chooses),
-                                   PSV_KERNELS_DIRECT, PSV_KERNELS_TMA or PSV_KERNELS_VEC4
-                                   (the last two FP32 only) */
+                                   PSV_KERNELS_DIRECT, _TMA, _VEC4 or _FUSED (the last three
+                                   FP32 only; FUSED needs no free surface but a top one) */
     int autotune;               /* 1 (default): time the tile-shape candidates on the first
                                    time loop and keep the fastest (psv_plan_autotune);
                                    0: use block_y / rows_per_thread as given */
@@ -300,7 +302,8 @@ int psv_last_timing(const psv_plan *plan, double *ms3);
 int psv_plan_autotune(psv_plan *plan, int nsteps, int *kernel_family, int *rows_per_thread,
                       int *block_y);
 /* The time-step kernels the plan launches now: family (PSV_KERNELS_*), rows
- * per thread and block height (any pointer may be NULL). */
+ * per thread (FUSED: tile rows) and block height (TMA: 4, FUSED: 0); any
+ * pointer may be NULL. */
 int psv_plan_shape(const psv_plan *plan, int *kernel_family, int *rows_per_thread, int *block_y);
 /* The plan's snapshot storage: PSV_STORE_FULL, _CHECKPOINT or _BINOMIAL
  * (never AUTO), steps per segment and state slots per shot (0 for FULL),

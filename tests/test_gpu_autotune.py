@@ -31,7 +31,8 @@ def test_autotune_shape_and_parity(gpu, orc):
         fam, rpt, by = p.autotune(8)
         assert (fam == "direct" and rpt in (1, 2, 4, -2, -4) and by in (2, 4, 8)) or \
                (fam == "tma" and rpt in (2, 4, 8)) or \
-               (fam == "vec4" and rpt in (1, 2, 4) and by in (2, 4, 8))
+               (fam == "vec4" and rpt in (1, 2, 4) and by in (2, 4, 8)) or \
+               (fam == "fused" and rpt in (16, 32) and by == 0)
         assert p.shape == (fam, rpt, by)
         L2, g = p.gradient()
     assert L2 == pytest.approx(L2_ref, rel=1e-4)
@@ -41,7 +42,8 @@ def test_autotune_shape_and_parity(gpu, orc):
 
 SHAPES = [("direct", 2, 4), ("direct", 4, 2), ("direct", -2, 4), ("direct", -4, 8),
           ("tma", 2, 0), ("tma", 4, 0), ("tma", 8, 0),
-          ("vec4", 1, 4), ("vec4", 2, 2), ("vec4", 4, 8)]
+          ("vec4", 1, 4), ("vec4", 2, 2), ("vec4", 4, 8),
+          ("fused", 16, 0), ("fused", 32, 0)]
 
 
 @pytest.mark.parametrize("fam,rpt,by", SHAPES)
@@ -61,7 +63,7 @@ def test_every_shape_gives_the_same_gradient(gpu, orc, fam, rpt, by, fdorder):
         assert helpers.rel_l2(b, a) < 1e-5
 
 
-@pytest.mark.parametrize("fam,rpt", [("tma", 4), ("vec4", 2)])
+@pytest.mark.parametrize("fam,rpt", [("tma", 4), ("vec4", 2), ("fused", 32), ("fused", 16)])
 @pytest.mark.parametrize("kw", [dict(fdorder=2, stencil="reference", nshot=3, nt=300),
                                 dict(fdorder=6, stencil="holberg", nshot=2, nt=250,
                                      imaging_sign=1),
@@ -93,13 +95,13 @@ def test_tiled_families_against_oracle(gpu, orc, kw, fam, rpt):
         assert helpers.rel_l2(a, b) < 1e-4
 
 
-@pytest.mark.parametrize("fam", ["tma", "vec4"])
+@pytest.mark.parametrize("fam", ["tma", "vec4", "fused"])
 def test_tiled_families_checkpointed_equal_full(gpu, orc, fam):
     sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=300, snap_dt=3)
     uz, ux = orc.simulate_fwd(sv, *true)
     out = []
     for storage, slots in (("full", 0), ("checkpoint", 0), ("binomial", 3)):
-        with engine.Plan(sv, precision=32, kernels=fam, rows_per_thread=2,
+        with engine.Plan(sv, precision=32, kernels=fam, rows_per_thread=16 if fam == "fused" else 2,
                          storage=storage, checkpoint_interval=40, checkpoint_slots=slots) as p:
             assert p.shape[0] == fam and p.storage[0] == storage
             p.set_model(*init)
@@ -110,3 +112,43 @@ def test_tiled_families_checkpointed_equal_full(gpu, orc, fam):
         assert La == Lb
         for a, b in zip(ga, gb):
             assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("rpt", [16, 32])
+def test_fused_step_without_free_surface(gpu, orc, rpt):
+    # CPML on all four sides (the top strip included), no free surface, odd
+    # step count (the pass ends on the second field copy), snapshots every
+    # third step
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nt=301, nshot=2, snap_dt=3)
+    sv.surf = False
+    sv.npml = (10, 10, 10, 10)
+    sv.finalize()
+    uz_ref, ux_ref = orc.simulate_fwd(sv, *true)
+    L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz_ref, ux_ref)
+    with engine.Plan(sv, precision=32, kernels="fused", rows_per_thread=rpt) as p:
+        assert p.shape == ("fused", rpt, 0)
+        p.set_model(*true)
+        uz, ux = p.forward()
+        assert helpers.rel_l2(uz, uz_ref) < 1e-5 and helpers.rel_l2(ux, ux_ref) < 1e-5
+        p.set_model(*init)
+        p.set_observed(uz_ref, ux_ref)
+        L2, g = p.gradient()
+    assert L2 == pytest.approx(L2_ref, rel=1e-4)
+    for a, b in zip(g, g_ref):
+        assert helpers.rel_l2(a, b) < 1e-4
+
+
+def test_fused_step_rejects_a_bottom_surface(gpu):
+    from fwi_cuda_gb300 import _lib
+    sv, true, _ = helpers.case(fdorder=4, stencil="holberg", nt=60)
+    sv.isurf = (0, sv.nz - 8, 0, 0)
+    sv.npml = (10, 0, 10, 10)
+    sv.z_src = np.full(sv.nsrc, 20, np.int32)
+    sv.z_rec = np.full(sv.nrec, sv.nz - 12, np.int32)
+    sv.finalize()
+    with pytest.raises(_lib.PSVError, match="fused"):
+        engine.Plan(sv, precision=32, kernels="fused")
+    with engine.Plan(sv, precision=32) as p:  # the autotuner leaves it out
+        p.set_model(*true)
+        p.set_observed(*p.forward())
+        assert p.autotune(4)[0] != "fused"
