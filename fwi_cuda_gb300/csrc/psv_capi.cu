@@ -4,6 +4,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <cstdlib>
 #include <vector>
 
 #include "psv_plan.cuh"
@@ -350,6 +351,53 @@ int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
         PSV_CU(cudaMemcpy(res_x, d[5].p, bytes, cudaMemcpyDeviceToHost));
     }
     return PSV_OK;
+}
+
+int psv_apply_gauss_filter(double *mat, int nz, int nx, int hfs)
+{
+    if (!mat || nz <= 0 || nx <= 0) return fail(PSV_ERR_ARG, "apply_gauss_filter: null array or bad size");
+    hfs = std::abs(hfs);
+    std::vector<double> k((size_t)(2 * hfs + 1) * (2 * hfs + 1));
+    PSV_TRY(psv_gauss_filter_kernel(hfs, k.data()));
+    if (!psv_device_available()) return fail(PSV_ERR_CUDA, "no CUDA device available");
+    const size_t bytes = (size_t)nz * nx * sizeof(double);
+    size_t total = 0;
+    DevMem a, b, f;
+    PSV_TRY(a.alloc(bytes, total));
+    PSV_TRY(b.alloc(bytes, total));
+    PSV_TRY(f.alloc(k.size() * sizeof(double), total));
+    PSV_CU(cudaMemcpy(a.p, mat, bytes, cudaMemcpyHostToDevice));
+    PSV_CU(cudaMemcpy(b.p, mat, bytes, cudaMemcpyHostToDevice));
+    PSV_CU(cudaMemcpy(f.p, k.data(), k.size() * sizeof(double), cudaMemcpyHostToDevice));
+    PSV_CU(launch_gauss_filter<double>(a.as<double>(), b.as<double>(), (long long)nz * nx, nx, nz,
+                                       nx, 1, f.as<double>(), hfs, 0));
+    PSV_CU(cudaMemcpy(mat, b.p, bytes, cudaMemcpyDeviceToHost));
+    return PSV_OK;
+}
+
+int psv_PCG_PSV(double *dir, double *old, double *grad, int nz, int nx)
+{
+    if (!dir || !old || !grad || nz <= 0 || nx <= 0)
+        return fail(PSV_ERR_ARG, "PCG_PSV: null array or bad size");
+    if (!psv_device_available()) return fail(PSV_ERR_CUDA, "no CUDA device available");
+    const long long n = (long long)nz * nx;
+    const size_t bytes = (size_t)n * sizeof(double);
+    size_t total = 0;
+    DevMem d[3], part;
+    for (auto &m : d) PSV_TRY(m.alloc(bytes, total));
+    PSV_TRY(part.alloc(2 * PCG_BLOCKS * sizeof(double), total));
+    double *h[3] = {dir, old, grad};
+    for (int k = 0; k < 3; k++) PSV_CU(cudaMemcpy(d[k].p, h[k], bytes, cudaMemcpyHostToDevice));
+    PSV_CU(launch_pcg(d[0].as<double>(), d[1].as<double>(), d[2].as<double>(), n,
+                      part.as<double>(), 0));
+    for (int k = 0; k < 3; k++) PSV_CU(cudaMemcpy(h[k], d[k].p, bytes, cudaMemcpyDeviceToHost));
+    return PSV_OK;
+}
+
+int psv_pcg_gradient(psv_plan *p)
+{
+    PLAN_CHECK(p);
+    return p->impl->pcg_gradient();
 }
 
 void *psv_plan_stream(const psv_plan *p) { return p && p->impl ? p->impl->stream() : nullptr; }

@@ -73,4 +73,18 @@ cudaError_t launch_update_mat(double *mat, const double *old, const double *grad
                               double mat_max, double mat_min, double step,
                               unsigned long long *maxbits2, cudaStream_t st);
 
+// apply_gauss_filter on nplanes planes of nz x nx values (row pitch `pitch`,
+// plane stride `plane`): dst at [hfs, nz - hfs - 1) x [hfs, nx - hfs - 1)
+// takes the (2 hfs + 1)^2 weighted sum of src in FP64 (filter row outer,
+// column inner); dst elsewhere is left alone.  filt is on the device.
+template <typename T>
+cudaError_t launch_gauss_filter(const T *src, T *dst, long long plane, int pitch, int nz, int nx,
+                                int nplanes, const double *filt, int hfs, cudaStream_t st);
+// PCG_PSV on n values: beta = |g|^2 / |old|^2 (0 when |old|^2 = 0, clipped
+// at 0), old <- -g, dir <- -g + beta dir, g <- dir.  part needs
+// 2 * PCG_BLOCKS doubles.
+constexpr int PCG_BLOCKS = 304;
+cudaError_t launch_pcg(double *dir, double *old, double *g, long long n, double *part,
+                       cudaStream_t st);
+
 }  // namespace psv

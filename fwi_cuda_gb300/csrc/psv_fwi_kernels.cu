@@ -442,6 +442,99 @@ cudaError_t launch_transpose(const double *in, double *out, int rows, int cols, 
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Optional preconditioners: Gaussian smoothing and the Fletcher-Reeves
+// direction (gauss_filter_kernel / apply_gauss_filter,
+// src/cpu/n_kernel_lib_PSV.cpp:1012-1084; PCG_PSV, src/cpu/n_PCG_PSV.cpp:13-44).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_gauss_filter(const T *src, T *dst, long long plane, int pitch, int nz, int nx,
+                               const double *filt, int hfs)
+{
+    const int ix = blockIdx.x * blockDim.x + threadIdx.x, iz = blockIdx.y * blockDim.y + threadIdx.y;
+    if (iz < hfs || iz >= nz - hfs - 1 || ix < hfs || ix >= nx - hfs - 1) return;
+    const T *s = src + (long long)blockIdx.z * plane;
+    const int n = 2 * hfs + 1;
+    double conv = 0.0;  // the reference's int accumulator truncates; see the header
+    for (int jj = 0; jj < n; jj++) {
+        const T *row = s + (long long)(iz + jj - hfs) * pitch + ix - hfs;
+        for (int ii = 0; ii < n; ii++) conv += (double)row[ii] * filt[jj * n + ii];
+    }
+    dst[(long long)blockIdx.z * plane + (long long)iz * pitch + ix] = (T)conv;
+}
+
+template <typename T>
+cudaError_t launch_gauss_filter(const T *src, T *dst, long long plane, int pitch, int nz, int nx,
+                                int nplanes, const double *filt, int hfs, cudaStream_t st)
+{
+    if (nplanes <= 0 || nz <= 0 || nx <= 0) return cudaSuccess;
+    const dim3 b(32, 8), g((nx + 31) / 32, (nz + 7) / 8, nplanes);
+    k_gauss_filter<T><<<g, b, 0, st>>>(src, dst, plane, pitch, nz, nx, filt, hfs);
+    return cudaGetLastError();
+}
+
+// Block partial sums of g^2 and old^2 (fixed grid: the same order every run).
+__global__ void k_pcg_sums(const double *g, const double *old, long long n, double *part)
+{
+    __shared__ double sa[256], sb[256];
+    double a = 0.0, b = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        a += g[i] * g[i];
+        b += old[i] * old[i];
+    }
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            sa[threadIdx.x] += sa[threadIdx.x + h];
+            sb[threadIdx.x] += sb[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = sa[0];
+        part[gridDim.x + blockIdx.x] = sb[0];
+    }
+}
+
+__global__ void k_pcg_apply(double *dir, double *old, double *g, long long n, const double *part)
+{
+    __shared__ double beta;
+    if (threadIdx.x == 0) {  // every block sums the partials in the same order
+        double bi = 0.0, bj = 0.0;
+        for (int k = 0; k < (int)gridDim.x; k++) {
+            bi += part[k];
+            bj += part[gridDim.x + k];
+        }
+        double b = bj > 0.0 ? bi / bj : 0.0;  // the reference divides by zero on its first call
+        beta = b > 0 ? b : 0.0;
+    }
+    __syncthreads();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double gi = g[i];
+        old[i] = -gi;
+        const double d = -gi + beta * dir[i];
+        dir[i] = d;
+        g[i] = d;
+    }
+}
+
+cudaError_t launch_pcg(double *dir, double *old, double *g, long long n, double *part,
+                       cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    k_pcg_sums<<<PCG_BLOCKS, 256, 0, st>>>(g, old, n, part);
+    k_pcg_apply<<<PCG_BLOCKS, 256, 0, st>>>(dir, old, g, n, part);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_gauss_filter<float>(const float *, float *, long long, int, int, int,
+                                                int, const double *, int, cudaStream_t);
+template cudaError_t launch_gauss_filter<double>(const double *, double *, long long, int, int,
+                                                 int, int, const double *, int, cudaStream_t);
 template cudaError_t launch_zero_planes<float>(float *, long long, long long, long long, int,
                                                cudaStream_t);
 template cudaError_t launch_zero_planes<double>(double *, long long, long long, long long, int,

@@ -272,6 +272,25 @@ extern "C" int psv_step_length(double *est_io, double L2_0, psv_trial_fn trial, 
     return PSV_OK;
 }
 
+extern "C" int psv_gauss_filter_kernel(int hfs, double *k)
+{
+    if (!k) return psv::fail(PSV_ERR_ARG, "gauss_filter_kernel: null filter");
+    hfs = std::abs(hfs);
+    if (hfs < 2) return psv::fail(PSV_ERR_ARG, "gauss_filter_kernel: hfs must be at least 2");
+    const int n = 2 * hfs + 1;
+    const double sigma = (double)(hfs / 2);  // the reference's integer division
+    const double q = 2.0 * sigma * sigma;
+    double sum = 0.0;
+    for (int ii = -hfs; ii <= hfs; ii++)  // x offset outer, as the reference sums
+        for (int jj = -hfs; jj <= hfs; jj++) {
+            const double v = std::exp(-((ii * ii) / q) - ((jj * jj) / q));
+            k[(size_t)(jj + hfs) * n + ii + hfs] = v;
+            sum += v;
+        }
+    for (int i = 0; i < n * n; i++) k[i] /= sum;
+    return PSV_OK;
+}
+
 extern "C" int psv_checkpoint_schedule(int nseg, int slots, int *actions, int cap, int *nactions,
                                        long long *advances)
 {

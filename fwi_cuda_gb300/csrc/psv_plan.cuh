@@ -134,6 +134,7 @@ struct PlanIface {
     virtual int fwi_iteration(double *step, double *L2, int *ntrials, double *tlog, int maxt) = 0;
     virtual int save_model() = 0;
     virtual int taper_gradient() = 0;
+    virtual int pcg_gradient() = 0;
     virtual int update_model(double step) = 0;
     virtual int trial_misfit(double step, double *L2) = 0;
     virtual int timing(double *ms3) const = 0;

@@ -71,6 +71,9 @@ public:
     long long ck_state = 0;  // elements of one shot's checkpointed state
     CkSchedule sched;
     std::vector<int> fwd_slot;  // per segment: slot the forward pass saves into, or -1
+    // Optional preconditioners: smoothing scratch and filter; Fletcher-Reeves
+    // state (dir, old for lam, mu, rho) and reduction partials.
+    DevMem gtmp, gfilt, pcgbuf, pcgpart;
     DevMem ck, fld2, memz2, memx2;
     StepParams<T> sp{}, sp2{};
     SrcRecParams<T> qf{}, qa{}, qk{}, qr{};
@@ -136,6 +139,8 @@ public:
             return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2, 3 or 4");
         if (opt.kernel_family >= PSV_KERNELS_TMA && sizeof(T) != 4)
             return fail(PSV_ERR_UNSUPPORTED, "TMA, VEC4 and FUSED kernels are FP32 only");
+        if (opt.smooth_hfs < 0 || opt.smooth_hfs == 1)
+            return fail(PSV_ERR_ARG, "smooth_hfs must be 0 (off) or at least 2");
         if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
         if (opt.block_y > 0 || opt.rows_per_thread) opt.autotune = 0;  // explicit shape wins
         if (opt.kernel_family == PSV_KERNELS_TMA) {
@@ -941,6 +946,7 @@ public:
             PSV_CU(cudaEventRecord(ev[2], st));
             PSV_TRY(run_pass(PASS_ADJ_RES));
             PSV_CU(cudaEventRecord(ev[3], st));
+            if (opt.smooth_hfs >= 2) PSV_TRY(smooth_shot_gradients(n));
             PSV_TRY(precondition(n));
             PSV_TRY(sync_check());
             float a, c, d;
@@ -957,6 +963,41 @@ public:
         for (int i = 0; i < nshot; i++) s += L2_shot[i];
         if (L2) *L2 = s;
         t_ms[0] = tf; t_ms[1] = ta; t_ms[2] = to;
+        return PSV_OK;
+    }
+
+    // apply_gauss_filter of the n batch shots' gradient planes (the
+    // reference's commented-out calls, n_simulate_PSV.cpp:377-379).
+    int smooth_shot_gradients(int n)
+    {
+        const int hfs = opt.smooth_hfs;
+        if (!gfilt.p) {
+            std::vector<double> k((size_t)(2 * hfs + 1) * (2 * hfs + 1));
+            PSV_TRY(psv_gauss_filter_kernel(hfs, k.data()));
+            PSV_TRY(gfilt.alloc(k.size() * sizeof(double), total));
+            PSV_CU(cudaMemcpy(gfilt.p, k.data(), k.size() * sizeof(double), cudaMemcpyHostToDevice));
+            PSV_TRY(gtmp.alloc((size_t)B * gshot_shot * sizeof(T), total));
+        }
+        const size_t bytes = (size_t)n * gshot_shot * sizeof(T);
+        PSV_CU(cudaMemcpyAsync(gtmp.p, gshot.p, bytes, cudaMemcpyDeviceToDevice, st));
+        PSV_CU(launch_gauss_filter<T>(gtmp.as<T>(), gshot.as<T>(), sp.snap_plane, snx_pitch, sv.snz,
+                                      sv.snx, 3 * n, gfilt.as<double>(), hfs, st));
+        return PSV_OK;
+    }
+
+    // PCG_PSV x3 on the global gradients (n_simulate_PSV.cpp:433-435).
+    int pcg_gradient() override
+    {
+        const long long n = (long long)sv.g.nz * sv.g.nx;
+        if (!pcgbuf.p) {
+            PSV_TRY(pcgbuf.alloc((size_t)6 * n * sizeof(double), total));
+            PSV_TRY(pcgpart.alloc(2 * PCG_BLOCKS * sizeof(double), total));
+            PSV_CU(cudaMemsetAsync(pcgbuf.p, 0, pcgbuf.bytes, st));
+        }
+        double *d = pcgbuf.as<double>();
+        for (int k = 0; k < 3; k++)
+            PSV_CU(launch_pcg(d + (size_t)k * n, d + (size_t)(3 + k) * n, grad(k), n,
+                              pcgpart.as<double>(), st));
         return PSV_OK;
     }
 
@@ -1124,6 +1165,7 @@ public:
         PSV_TRY(gradient(&L2));
         if (L2out) *L2out = L2;
         PSV_CU(cudaEventRecord(ev[0], st));
+        if (opt.pcg) PSV_TRY(pcg_gradient());
         PSV_TRY(taper_gradient());
         // step_length_PSV (src/cpu/n_step_length_PSV.cpp:53-209), update_param 0.
         double est = *step;

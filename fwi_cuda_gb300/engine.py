@@ -25,7 +25,7 @@ FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused"}
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
             block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
-            kernels="any", checkpoint_slots=0) -> PsvOptions:
+            kernels="any", checkpoint_slots=0, smooth_hfs=0, pcg=False) -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -36,10 +36,34 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.block_x, o.block_y = int(block[0]), int(block[1])
     o.checkpoint_interval = int(checkpoint_interval)
     o.checkpoint_slots = int(checkpoint_slots)
+    o.smooth_hfs = int(smooth_hfs)
+    o.pcg = int(bool(pcg))
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
     o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4}[kernels]
     return o
+
+
+def gauss_filter_kernel(hfs):
+    """gauss_filter_kernel: the (2 hfs + 1)^2 smoothing weights (host only)."""
+    k = np.zeros((2 * abs(hfs) + 1, 2 * abs(hfs) + 1))
+    check(_lib.lib().psv_gauss_filter_kernel(int(hfs), dptr(k)))
+    return k
+
+
+def apply_gauss_filter(mat, hfs):
+    """apply_gauss_filter: a smoothed copy of the [nz][nx] array."""
+    out = f64(mat).copy()
+    check(_lib.lib().psv_apply_gauss_filter(dptr(out), out.shape[0], out.shape[1], int(hfs)))
+    return out
+
+
+def PCG_PSV(dir_, old, grad):
+    """PCG_PSV: one Fletcher-Reeves step, the three float64 arrays updated in place."""
+    for a in (dir_, old, grad):
+        if a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise TypeError("PCG_PSV needs C-contiguous float64 arrays")
+    check(_lib.lib().psv_PCG_PSV(dptr(dir_), dptr(old), dptr(grad), grad.shape[0], grad.shape[1]))
 
 
 def checkpoint_schedule(nseg, slots):
@@ -161,6 +185,10 @@ class Plan:
 
     def taper_gradient(self):
         check(_lib.lib().psv_taper_gradient(self.h))
+
+    def pcg_gradient(self):
+        """PCG_PSV on the plan's global gradients (direction state kept by the plan)."""
+        check(_lib.lib().psv_pcg_gradient(self.h))
 
     def trial_misfit(self, step):
         L2 = C.c_double()

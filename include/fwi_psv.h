@@ -146,6 +146,13 @@ typedef struct psv_options {
     int checkpoint_slots;       /* BINOMIAL storage: state slots per shot (segment 0's
                                    included); 0 = the fewest with at most two forward
                                    repetitions, fewer if the budget holds fewer */
+    int smooth_hfs;             /* >= 2: Gaussian smoothing (half size hfs) of every shot's
+                                   gradients before the energy preconditioning, where the
+                                   reference's commented-out apply_gauss_filter calls sit
+                                   (src/cpu/n_simulate_PSV.cpp:377-379); 0 = off */
+    int pcg;                    /* 1: psv_fwi_iteration turns the global gradients into
+                                   Fletcher-Reeves directions before the taper (the
+                                   reference's commented-out PCG_PSV calls, :433-435) */
 } psv_options;
 
 void psv_options_default(psv_options *opt);
@@ -269,6 +276,21 @@ int psv_step_length(double *est, double L2_0, psv_trial_fn trial, void *ctx, int
  * past its arrays, include/cpu/n_solvelin.hpp:37-42). */
 double psv_calc_opt_step(const double *L2, const double *sl);
 
+/* Optional preconditioners (dead code in the reference, available here):
+ *   psv_gauss_filter_kernel: gauss_filter_kernel (src/cpu/n_kernel_lib_PSV.cpp:1012):
+ *     filter[(2 hfs + 1)^2], row = z offset + hfs, column = x offset + hfs,
+ *     sigma = hfs / 2 in integer arithmetic as the reference computes it;
+ *     hfs < 2 is PSV_ERR_ARG (the reference's weights are NaN there).  Host only.
+ *   psv_apply_gauss_filter: apply_gauss_filter (:1053) on a host [nz][nx] array,
+ *     in place, on the device; the filtered sums are FP64 (the reference
+ *     accumulates into an int, truncating every partial sum).
+ *   psv_PCG_PSV: PCG_PSV (src/cpu/n_PCG_PSV.cpp:13), Fletcher-Reeves, on host
+ *     [nz][nx] arrays updated in place, on the device; beta = 0 when |old|^2 = 0
+ *     (the reference divides by zero on its first call). */
+int psv_gauss_filter_kernel(int hfs, double *filter);
+int psv_apply_gauss_filter(double *mat, int nz, int nx, int hfs);
+int psv_PCG_PSV(double *dir, double *old, double *grad, int nz, int nx);
+
 /* The pieces of psv_fwi_iteration, for drivers that split the shots of a
  * survey over several plans / GPUs and reduce between them:
  *   psv_save_model      copy_mat: the model trials and the update start from
@@ -284,6 +306,9 @@ double psv_calc_opt_step(const double *L2, const double *sl);
  * all-reduced, update. */
 int psv_save_model(psv_plan *plan);
 int psv_taper_gradient(psv_plan *plan);
+/* PCG_PSV on the plan's three global gradients with the plan's direction
+ * state (zero before the first call), as psv_PCG_PSV. */
+int psv_pcg_gradient(psv_plan *plan);
 int psv_trial_misfit(psv_plan *plan, double step, double *L2);
 int psv_update_model(psv_plan *plan, double step);
 

@@ -127,6 +127,10 @@ class Lib:
             f("checkfd_ssg_elastic").restype = C.c_int
             f("step_length_cb").argtypes = [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp]
             f("step_length_cb").restype = C.c_int
+            f("gauss_filter_kernel").argtypes = [C.c_int, _dp]
+            f("gauss_filter_kernel").restype = C.c_int
+            f("apply_gauss_filter").argtypes = [_dp, C.c_int, C.c_int, _dp, C.c_int]
+            f("PCG_PSV").argtypes = [_dp, _dp, _dp, C.c_int, C.c_int]
         else:
             f("taper2").argtypes = [_dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _ip]
             f("interpol_grad2").argtypes = [_dp, _dp] + [C.c_int] * 8
@@ -268,6 +272,25 @@ class Lib:
         out["rtf_uz"], out["rtf_ux"] = rtf_uz, rtf_ux
         out["history"] = history
         return out
+
+    def gauss_filter_kernel(self, hfs):
+        k = np.zeros((2 * abs(hfs) + 1, 2 * abs(hfs) + 1))
+        if self.fn("gauss_filter_kernel")(int(hfs), dptr(k)) != 0:
+            raise ValueError("hfs must be at least 2")
+        return k
+
+    def apply_gauss_filter(self, mat, hfs):
+        """Filtered copy of mat (orc_ only)."""
+        out = _f64(mat).copy()
+        k = self.gauss_filter_kernel(hfs)
+        self.fn("apply_gauss_filter")(dptr(out), out.shape[0], out.shape[1], dptr(k), int(hfs))
+        return out
+
+    def PCG_PSV(self, dir_, old, grad):
+        """One Fletcher-Reeves step; updates the three arrays in place (orc_ only)."""
+        for a in (dir_, old, grad):
+            assert a.dtype == np.float64 and a.flags.c_contiguous
+        self.fn("PCG_PSV")(dptr(dir_), dptr(old), dptr(grad), grad.shape[0], grad.shape[1])
 
     def shot_gradient(self, case, ishot, lam, mu, rho, true_uz, true_ux):
         """Forward + residual + adjoint of one shot (orc_ only)."""

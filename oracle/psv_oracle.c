@@ -404,6 +404,72 @@ void orc_taper2(double *A, int nz, int nx, int snap_z1, int snap_z2, int snap_x1
         }
 }
 
+/* gauss_filter_kernel, src/cpu/n_kernel_lib_PSV.cpp:1012-1050: (2 hfs + 1)^2
+ * weights exp(-(i^2 / q) - (j^2 / q)), q = 2 sigma^2, sigma = hfs / 2 in
+ * integer arithmetic as the reference writes it, normalised by their sum
+ * (accumulated with the x offset outer).  Row jj + hfs, column ii + hfs.
+ * hfs < 2 is rejected (-1): the reference's sigma is 0 there and its
+ * weights are NaN. */
+int orc_gauss_filter_kernel(int hfs, double *k)
+{
+    if (hfs < 0) hfs = -hfs;
+    if (hfs < 2) return -1;
+    const int n = 2 * hfs + 1;
+    const double sigma = (double)(hfs / 2);
+    const double q = 2.0 * sigma * sigma;
+    double sum = 0.0;
+    for (int ii = -hfs; ii <= hfs; ii++)
+        for (int jj = -hfs; jj <= hfs; jj++) {
+            const double v = exp(-((ii * ii) / q) - ((jj * jj) / q));
+            k[(size_t)(jj + hfs) * n + ii + hfs] = v;
+            sum += v;
+        }
+    for (int i = 0; i < n * n; i++) k[i] /= sum;
+    return 0;
+}
+
+/* apply_gauss_filter, src/cpu/n_kernel_lib_PSV.cpp:1053-1084: points
+ * [hfs, nz - hfs - 1) x [hfs, nx - hfs - 1) take the filtered value of a copy
+ * of mat (rows outer, filter row jj outer, column ii inner); the others keep
+ * theirs.  The sum is a double: the reference accumulates into an int,
+ * which truncates every partial sum (gradients become 0, moduli overflow). */
+void orc_apply_gauss_filter(double *mat, int nz, int nx, const double *filt, int hfs)
+{
+    const int n = 2 * hfs + 1;
+    double *tmp = zalloc((size_t)nz * nx);
+    memcpy(tmp, mat, sizeof(double) * (size_t)nz * nx);
+    for (int iz = hfs; iz < nz - hfs - 1; iz++)
+        for (int ix = hfs; ix < nx - hfs - 1; ix++) {
+            double conv = 0.0;
+            for (int jj = 0; jj < n; jj++)
+                for (int ii = 0; ii < n; ii++)
+                    conv += tmp[IDX(iz + jj - hfs, ix + ii - hfs, nx)] * filt[(size_t)jj * n + ii];
+            mat[IDX(iz, ix, nx)] = conv;
+        }
+    free(tmp);
+}
+
+/* PCG_PSV, src/cpu/n_PCG_PSV.cpp:13-44 (Fletcher-Reeves): beta = |grad|^2 /
+ * |old|^2, negative beta -> 0; old <- -grad; dir <- -grad + beta dir;
+ * grad <- dir.  When |old|^2 = 0 (the first call, old starts at zero) beta
+ * is 0: the reference divides by zero there and its direction is NaN. */
+void orc_PCG_PSV(double *dir, double *old, double *grad, int nz, int nx)
+{
+    const size_t n = (size_t)nz * nx;
+    double bi = 0.0, bj = 0.0;
+    for (size_t i = 0; i < n; i++) {
+        bi += grad[i] * grad[i];
+        bj += old[i] * old[i];
+        old[i] = -grad[i];
+    }
+    double beta = bj > 0.0 ? bi / bj : 0.0;
+    beta = beta > 0 ? beta : 0.0;
+    for (size_t i = 0; i < n; i++) {
+        dir[i] = -grad[i] + beta * dir[i];
+        grad[i] = dir[i];
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Time-loop building blocks                                                */
 /* ------------------------------------------------------------------------ */

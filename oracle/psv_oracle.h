@@ -88,6 +88,9 @@ void orc_scale_grad_E2(double *grad, const double *grad_shot, double mat_av, con
                        int nx, int snap_z1, int snap_z2, int snap_x1, int snap_x2);
 void orc_update_mat2(double *mat, const double *mat_old, const double *grad_mat, double mat_max,
                      double mat_min, double step_length, int nz, int nx);
+int orc_gauss_filter_kernel(int hfs, double *k);
+void orc_apply_gauss_filter(double *mat, int nz, int nx, const double *filt, int hfs);
+void orc_PCG_PSV(double *dir, double *old, double *grad, int nz, int nx);
 void orc_taper2(double *A, int nz, int nx, int snap_z1, int snap_z2, int snap_x1, int snap_x2,
                 const int *taper8 /* t1 t2 b1 b2 l1 l2 r1 r2 */);
 

@@ -73,9 +73,11 @@ def load_case(z, name):
     return S.Survey(**kw).finalize()
 
 
-def oracle_gradient(orc, sv, model, obs_uz, obs_ux):
+def oracle_gradient(orc, sv, model, obs_uz, obs_ux, smooth_hfs=0):
     """Global gradients of one FWI gradient pass (simulate_fwi_PSV :270-417)
-    from the oracle's building blocks, before the taper."""
+    from the oracle's building blocks, before the taper; smooth_hfs >= 2
+    smooths every shot gradient first (the commented-out apply_gauss_filter
+    calls, :377-379)."""
     lam, mu, rho = model
     _, _, _, Cs = orc.mat_av2(lam, mu, rho)
     snap = (sv.snap_z1, sv.snap_z2, sv.snap_x1, sv.snap_x2)
@@ -88,6 +90,8 @@ def oracle_gradient(orc, sv, model, obs_uz, obs_ux):
         L2 += o["L2"]
         We = orc.energy_weights2(o["We"], o["We_adj"], snap)
         for p, k in enumerate(("grad_lam", "grad_mu", "grad_rho")):
+            if smooth_hfs:
+                o[k] = orc.apply_gauss_filter(o[k], smooth_hfs)
             tmp = orc.interpol_grad2(o["We_adj"], o[k], snap, sv.snap_dz, sv.snap_dx)
             grads[p] = orc.scale_grad_E2(grads[p], tmp, Cs[p], We, snap)
     return L2, grads, shots
