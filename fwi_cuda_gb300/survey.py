@@ -208,6 +208,112 @@ def smoothed(vp, sigma, vs_ratio=1.73):
     return model_from_vp(gaussian_filter(vp, sigma, mode="nearest"), vs_ratio)
 
 
+# ----------------------------------------------------------------------------
+# Field geometry (topography and acquisition coordinates)
+# ----------------------------------------------------------------------------
+
+def v_lami(cp, cs, rho):
+    """Lame constants from velocities (scripts/seismic_def.py, v_lami)."""
+    mu = cs * cs * rho
+    return cp * cp * rho - 2.0 * mu, mu
+
+
+def e_lami(E, nu):
+    """Lame constants from Young's modulus and Poisson's ratio (e_lami)."""
+    return E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), 0.5 * E / (1.0 + nu)
+
+
+def w_vel(lam, mu, rho):
+    """P and S velocities from Lame constants and density (w_vel)."""
+    return np.sqrt((lam + 2 * mu) / rho), np.sqrt(mu / rho)
+
+
+@dataclass
+class Topography:
+    """A ground profile on the model grid: nz x nx cells of dz x dx, the x
+    coordinate of column 0 and the first ground row of every column."""
+    nz: int
+    nx: int
+    xmin: float
+    dz: float
+    dx: float
+    surf_idz: np.ndarray  # [nx] int
+
+    def cell_x(self, x):
+        """Column of each x coordinate (floor, as the reference's int())."""
+        return ((np.asarray(x, np.float64) - self.xmin) / self.dx).astype(np.int32)
+
+    def on_surface(self, x):
+        """(z, x) grid indices of points placed on the ground at x."""
+        ix = self.cell_x(x)
+        if ix.size and (ix.min() < 0 or ix.max() >= self.nx):
+            raise ValueError("a coordinate lies outside the model")
+        return self.surf_idz[ix].astype(np.int32), ix
+
+
+def topography_grid(profile_x, profile_z, x0, x1, dz, dx, *, npml=(20, 20, 20, 20), fpad=1,
+                    z_above=10, z_below=20) -> Topography:
+    """Grid around a ground profile (elevations profile_z at profile_x, in
+    metres, up positive), the layout of scripts/pre_proc_dyke_4000.py:93-130:
+    columns for [x0, x1] plus CPML (npml = top, bottom, left, right) and fpad
+    cells; rows for the profile's relief plus z_above air and z_below ground
+    cells, CPML and fpad; the profile is flipped to depths, shifted below
+    the added rows and interpolated linearly at every column centre (the
+    edge elevations continue beyond the profile's ends, where the
+    reference's interpolation raises)."""
+    pt, pb, pl, pr = npml
+    px = np.asarray(profile_x, np.float64)
+    depth = np.max(profile_z) - np.asarray(profile_z, np.float64)  # top at depth 0
+    relief = abs(float(np.max(profile_z) - np.min(profile_z)))
+    nx = fpad + pl + int(abs(x1 - x0) / dx) + pr + fpad + 1
+    nz = fpad + pt + z_above + int(relief / dz) + z_below + pb + fpad + 1
+    xmin = x0 - (pl + fpad) * dx
+    xmax = x1 + (pr + fpad) * dx
+    zmin = np.min(depth) - (z_above + pt + fpad) * dz
+    depth = depth + (np.min(depth) - zmin)
+    order = np.argsort(px)
+    zc = np.interp(np.linspace(xmin, xmax, nx), px[order], depth[order])
+    return Topography(nz=nz, nx=nx, xmin=xmin, dz=dz, dx=dx,
+                      surf_idz=(zc / dz).astype(np.int64))
+
+
+def topography_model(topo: Topography, ground, air=(0.0, 0.0, 1.25), *, layers=(),
+                     perturb=0.0, sigma=0.0, rng=None):
+    """lam, mu, rho of a model with air above the ground profile and the
+    ground material (cp, cs, rho) below it; layers = ((depth_m, cp, cs, rho),
+    ...) put other materials within depth_m of the surface, in order; perturb
+    scales every cell by 1 + perturb * U(-1, 1); sigma > 0 smooths with a
+    Gaussian (constant mode) and restores the air, as
+    scripts/pre_proc_dyke_4000.py:170-205 does."""
+    from scipy.ndimage import gaussian_filter
+    rng = rng if rng is not None else np.random.default_rng(0)
+    iz = np.arange(topo.nz)[:, None]
+    below = iz >= topo.surf_idz[None, :]
+    out = []
+    for k in range(3):
+        def prop(m):
+            lam, mu = v_lami(m[0], m[1], m[2])
+            return (lam, mu, m[2])[k]
+        a = np.where(below, prop(ground), prop(air)).astype(np.float64)
+        for depth_m, *m in layers:
+            inside = below & (iz < topo.surf_idz[None, :] + depth_m / topo.dz)
+            a = np.where(inside, prop(m), a)
+        if perturb:
+            a = np.where(below, a * (1.0 + perturb * rng.uniform(-1, 1, a.shape)), a)
+        if sigma:
+            a = gaussian_filter(a, sigma, mode="constant")
+            a = np.where(below, a, prop(air))
+        out.append(a)
+    return tuple(out)
+
+
+def load_profile_csv(path):
+    """A ground profile file of the reference's layout (two comma-separated
+    columns x, z; scripts/pre_proc_dyke_4000.py:45): (x, z)."""
+    xz = np.loadtxt(path, delimiter=",").T
+    return xz[0], xz[1]
+
+
 def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml=20, nshot=1,
                    nrec=120, rec_spacing=4, src_depth=4, rec_depth=2, fc=100.0, vp_max=3000.0,
                    snap_dt=1, surf_offset=None, force="z", seed=0) -> Survey:
