@@ -492,6 +492,51 @@ __device__ __forceinline__ void velocity_point(const StepParams<T> &p, int bz, i
         snapshot_point<T, MODE>(p, bz, iz, ix, i, slot, ozz, ozx, oxx, vzn, vxn, uzn, uxn);
 }
 
+// Stress update of rows zb .. zb + RPT - 1 of column ix of a block lying in
+// the interior, away from the free surfaces and the rows / columns they
+// mirror: unchecked loads with 32-bit offsets (stencil neighbours are inside
+// the grid).  CPML: the block touches an absorbing strip, and the points in
+// it apply pml_diff2 (cpml_stress skips the others).
+template <typename T, int NS, int RPT, bool CPML>
+__device__ __forceinline__ void stress_rows_inner(const StepParams<T> &p, T *f, int bz, int zb,
+                                                  int ix)
+{
+    const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
+    const T *__restrict__ vzc = f + F_VZ * pl + i0;
+    const T *__restrict__ vxc = f + F_VX * pl + i0;
+    T *__restrict__ szz = f + F_SZZ * pl;
+    constexpr int W = RPT + 2 * NS - 1;
+    T wz[W], wx[W];  // wz[j] = vz[zb - N + j], wx[j] = vx[zb - N + 1 + j]
+#pragma unroll
+    for (int j = 0; j < W; j++) {
+        wz[j] = vzc[(j - NS) * P];
+        wx[j] = vxc[(j - NS + 1) * P];
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+        const T *vzr = vzc + r * P, *vxr = vxc + r * P;
+        const T oz = wz[r + NS], ox = wx[r + NS - 1];
+        T vz_z = p.cz[0] * (oz - wz[r + NS - 1]);
+        T vx_z = p.cz[0] * (wx[r + NS] - ox);
+        T vz_x = p.cx[0] * (vzr[1] - oz);
+        T vx_x = p.cx[0] * (ox - vxr[-1]);
+#pragma unroll
+        for (int k = 2; k <= NS; k++) {
+            vz_z += p.cz[k - 1] * (wz[r + NS + k - 1] - wz[r + NS - k]);
+            vx_z += p.cz[k - 1] * (wx[r + NS + k - 1] - wx[r + NS - k]);
+            vz_x += p.cx[k - 1] * (vzr[k] - vzr[-(k - 1)]);
+            vx_x += p.cx[k - 1] * (vxr[k - 1] - vxr[-k]);
+        }
+        if constexpr (CPML) cpml_stress(p, bz, zb + r, ix, vz_z, vx_z, vz_x, vx_x);
+        const int i = i0 + r * P;
+        const T cl = p.c_lam[i], c2 = p.c_l2m[i], cm = p.c_muzx[i];
+        const T ozz = szz[i], ozx = szz[i + pl], oxx = szz[i + 2 * pl];
+        szz[i] = ozz + (c2 * vz_z + cl * vx_x);
+        szz[i + 2 * pl] = oxx + (cl * vz_z + c2 * vx_x);
+        szz[i + pl] = ozx + cm * (vz_x + vx_z);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Stress step, direct loads: vdiff2 + pml_diff2 + update_s2 + surf_mirror
 // (src/cpu/n_kernel_lib_PSV.cpp:100-131, 134-205, 272-395).  Interior points
@@ -508,41 +553,14 @@ __global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
     T *f = p.fld + (long long)bp.bz * p.shot_stride;
     {
         const int bz0 = p.nz1 + bp.by * blockDim.y * RPT, bx0 = p.nx1 + bp.bx * 32;
-        if (plain_stress_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32)) {
+        const int bz1 = bz0 + (int)blockDim.y * RPT, bx1 = bx0 + 32;
+        if (plain_stress_box(p, bz0, bz1, bx0, bx1)) {
             // no bounds, CPML or surface work: 32-bit offsets, unpredicated loads
-            const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
-            const T *__restrict__ vzc = f + F_VZ * pl + i0;
-            const T *__restrict__ vxc = f + F_VX * pl + i0;
-            T *__restrict__ szz = f + F_SZZ * pl;
-            constexpr int W = RPT + 2 * NS - 1;
-            T wz[W], wx[W];  // wz[j] = vz[zb - N + j], wx[j] = vx[zb - N + 1 + j]
-#pragma unroll
-            for (int j = 0; j < W; j++) {
-                wz[j] = vzc[(j - NS) * P];
-                wx[j] = vxc[(j - NS + 1) * P];
-            }
-#pragma unroll
-            for (int r = 0; r < RPT; r++) {
-                const T *vzr = vzc + r * P, *vxr = vxc + r * P;
-                const T oz = wz[r + NS], ox = wx[r + NS - 1];
-                T vz_z = p.cz[0] * (oz - wz[r + NS - 1]);
-                T vx_z = p.cz[0] * (wx[r + NS] - ox);
-                T vz_x = p.cx[0] * (vzr[1] - oz);
-                T vx_x = p.cx[0] * (ox - vxr[-1]);
-#pragma unroll
-                for (int k = 2; k <= NS; k++) {
-                    vz_z += p.cz[k - 1] * (wz[r + NS + k - 1] - wz[r + NS - k]);
-                    vx_z += p.cz[k - 1] * (wx[r + NS + k - 1] - wx[r + NS - k]);
-                    vz_x += p.cx[k - 1] * (vzr[k] - vzr[-(k - 1)]);
-                    vx_x += p.cx[k - 1] * (vxr[k - 1] - vxr[-k]);
-                }
-                const int i = i0 + r * P;
-                const T cl = p.c_lam[i], c2 = p.c_l2m[i], cm = p.c_muzx[i];
-                const T ozz = szz[i], ozx = szz[i + pl], oxx = szz[i + 2 * pl];
-                szz[i] = ozz + (c2 * vz_z + cl * vx_x);
-                szz[i + 2 * pl] = oxx + (cl * vz_z + c2 * vx_x);
-                szz[i + pl] = ozx + cm * (vz_x + vx_z);
-            }
+            stress_rows_inner<T, NS, RPT, false>(p, f, bp.bz, zb, ix);
+            return;
+        }
+        if (inner_stress_box(p, bz0, bz1, bx0, bx1)) {  // CPML strip, no bounds or surface work
+            stress_rows_inner<T, NS, RPT, true>(p, f, bp.bz, zb, ix);
             return;
         }
     }
@@ -593,6 +611,63 @@ __global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
     }
 }
 
+// Velocity update (with the step's snapshot store / imaging) of rows
+// zb .. zb + RPT - 1 of column ix of a block lying in the interior:
+// unchecked loads with 32-bit offsets, imaging loads issued first.  CPML:
+// the block touches an absorbing strip, and the points in it apply
+// pml_diff2 (cpml_velocity skips the others).
+template <typename T, int NS, int MODE, int RPT, bool CPML>
+__device__ __forceinline__ void velocity_rows_inner(const StepParams<T> &p, T *f, int bz, int zb,
+                                                    int ix, int slot)
+{
+    constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
+    const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
+    const T *__restrict__ zzc = f + F_SZZ * pl + i0;
+    const T *__restrict__ zxc = f + F_SZX * pl + i0;
+    const T *__restrict__ xxc = f + F_SXX * pl + i0;
+    constexpr int W = RPT + 2 * NS - 1;
+    const bool image = MODE == MODE_ADJ && slot >= 0;
+    ImagePre<T> pre[RPT];  // imaging loads first: their latency overlaps the stencil loads
+#pragma unroll
+    for (int r = 0; r < RPT; r++)
+        if (image) pre[r] = image_preload(p, bz, zb + r, ix, i0 + r * P, slot);
+    T wzz[W], wzx[W];  // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
+#pragma unroll
+    for (int j = 0; j < W; j++) {
+        wzz[j] = zzc[(j - NS + 1) * P];
+        wzx[j] = zxc[(j - NS) * P];
+    }
+#pragma unroll
+    for (int r = 0; r < RPT; r++) {
+        const T *zxr = zxc + r * P, *xxr = xxc + r * P;
+        const T ozz = wzz[r + NS - 1], ozx = wzx[r + NS], oxx = xxr[0];
+        T szz_z = p.cz[0] * (wzz[r + NS] - ozz);
+        T szx_z = p.cz[0] * (ozx - wzx[r + NS - 1]);
+        T szx_x = p.cx[0] * (ozx - zxr[-1]);
+        T sxx_x = p.cx[0] * (xxr[1] - oxx);
+#pragma unroll
+        for (int k = 2; k <= NS; k++) {
+            szz_z += p.cz[k - 1] * (wzz[r + NS + k - 1] - wzz[r + NS - k]);
+            szx_z += p.cz[k - 1] * (wzx[r + NS + k - 1] - wzx[r + NS - k]);
+            szx_x += p.cx[k - 1] * (zxr[k - 1] - zxr[-k]);
+            sxx_x += p.cx[k - 1] * (xxr[k] - xxr[-(k - 1)]);
+        }
+        if constexpr (CPML) cpml_velocity(p, bz, zb + r, ix, szz_z, szx_z, szx_x, sxx_x);
+        const int i = i0 + r * P;
+        const T uzo = U ? f[F_UZ * pl + i] : T(0), uxo = U ? f[F_UX * pl + i] : T(0);
+        const T weo = MODE != MODE_FWD_NOWE ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * pl + i] : T(0);
+        T vzn, vxn, uzn = T(0), uxn = T(0);
+        velocity_finish<T, MODE>(p, f, i, f[F_VZ * pl + i], f[F_VX * pl + i], uzo, uxo, weo,
+                                 p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x, sxx_x, vzn, vxn,
+                                 uzn, uxn);
+        if (image)
+            image_apply(p, bz, pre[r], ozz, ozx, oxx, uzn, uxn);
+        else if (slot >= 0)
+            snapshot_point<T, MODE>(p, bz, zb + r, ix, i, slot, ozz, ozx, oxx,
+                                    vzn, vxn, uzn, uxn);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Velocity step, direct loads: sdiff2 + pml_diff2 + update_v2
 // (src/cpu/n_kernel_lib_PSV.cpp:207-270, 134-178), fused with the step's
@@ -623,51 +698,9 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
     const bool plain = plain_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32);
 
     if (plain) {  // interior, no CPML: 32-bit offsets, unpredicated loads
-        constexpr bool U = MODE == MODE_ADJ || MODE == MODE_FWD_U;
-        const int P = p.pitch, pl = (int)p.plane, i0 = zb * P + ix;
-        const T *__restrict__ zzc = f + F_SZZ * pl + i0;
-        const T *__restrict__ zxc = f + F_SZX * pl + i0;
-        const T *__restrict__ xxc = f + F_SXX * pl + i0;
-        constexpr int W = RPT + 2 * NS - 1;
-        const bool image = MODE == MODE_ADJ && slot >= 0;
-        ImagePre<T> pre[RPT];  // imaging loads first: their latency overlaps the stencil loads
-#pragma unroll
-        for (int r = 0; r < RPT; r++)
-            if (image) pre[r] = image_preload(p, bp.bz, zb + r, ix, i0 + r * P, slot);
-        T wzz[W], wzx[W];  // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
-#pragma unroll
-        for (int j = 0; j < W; j++) {
-            wzz[j] = zzc[(j - NS + 1) * P];
-            wzx[j] = zxc[(j - NS) * P];
-        }
-#pragma unroll
-        for (int r = 0; r < RPT; r++) {
-            const T *zxr = zxc + r * P, *xxr = xxc + r * P;
-            const T ozz = wzz[r + NS - 1], ozx = wzx[r + NS], oxx = xxr[0];
-            T szz_z = p.cz[0] * (wzz[r + NS] - ozz);
-            T szx_z = p.cz[0] * (ozx - wzx[r + NS - 1]);
-            T szx_x = p.cx[0] * (ozx - zxr[-1]);
-            T sxx_x = p.cx[0] * (xxr[1] - oxx);
-#pragma unroll
-            for (int k = 2; k <= NS; k++) {
-                szz_z += p.cz[k - 1] * (wzz[r + NS + k - 1] - wzz[r + NS - k]);
-                szx_z += p.cz[k - 1] * (wzx[r + NS + k - 1] - wzx[r + NS - k]);
-                szx_x += p.cx[k - 1] * (zxr[k - 1] - zxr[-k]);
-                sxx_x += p.cx[k - 1] * (xxr[k] - xxr[-(k - 1)]);
-            }
-            const int i = i0 + r * P;
-            const T uzo = U ? f[F_UZ * pl + i] : T(0), uxo = U ? f[F_UX * pl + i] : T(0);
-            const T weo = MODE != MODE_FWD_NOWE ? f[(MODE == MODE_ADJ ? F_WEA : F_WE) * pl + i] : T(0);
-            T vzn, vxn, uzn = T(0), uxn = T(0);
-            velocity_finish<T, MODE>(p, f, i, f[F_VZ * pl + i], f[F_VX * pl + i], uzo, uxo, weo,
-                                     p.c_rz[i], p.c_rx[i], szz_z, szx_z, szx_x, sxx_x, vzn, vxn,
-                                     uzn, uxn);
-            if (image)
-                image_apply(p, bp.bz, pre[r], ozz, ozx, oxx, uzn, uxn);
-            else if (slot >= 0)
-                snapshot_point<T, MODE>(p, bp.bz, zb + r, ix, i, slot, ozz, ozx, oxx,
-                                        vzn, vxn, uzn, uxn);
-        }
+        velocity_rows_inner<T, NS, MODE, RPT, false>(p, f, bp.bz, zb, ix, slot);
+    } else if (inner_box(p, bz0, bz0 + (int)blockDim.y * RPT, bx0, bx0 + 32)) {  // + CPML
+        velocity_rows_inner<T, NS, MODE, RPT, true>(p, f, bp.bz, zb, ix, slot);
     } else if (zb < p.nz) {  // warp-uniform
         // wzz[j] = szz[zb - N + 1 + j], wzx[j] = szx[zb - N + j]
         constexpr int W = RPT + 2 * NS - 1;
