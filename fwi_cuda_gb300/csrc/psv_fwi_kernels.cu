@@ -65,17 +65,33 @@ cudaError_t launch_coeffs(const CoeffParams<T> &c, cudaStream_t st)
 // ---------------------------------------------------------------------------
 // Deterministic block reductions.
 // ---------------------------------------------------------------------------
+// Butterfly sum of a warp's 32 values by register shuffles (every lane ends
+// with the same, order-fixed result).
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sum over the block: each warp by shuffles, then the warp sums by the
+// first warp; the same order on every run.  sh needs RED_THREADS / 32 + 1
+// doubles; every thread gets the result.
 __device__ __forceinline__ double block_sum(double v, double *sh)
 {
-    const int t = threadIdx.x;
-    sh[t] = v;
+    static_assert(RED_THREADS % 32 == 0 && RED_THREADS <= 1024, "whole warps");
+    constexpr int NW = RED_THREADS / 32;
+    const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+    v = warp_sum(v);
+    if (lane == 0) sh[w] = v;
     __syncthreads();
-    for (int s = RED_THREADS / 2; s > 0; s >>= 1) {
-        if (t < s) sh[t] = sh[t] + sh[t + s];
-        __syncthreads();
+    if (w == 0) {
+        double u = lane < NW ? sh[lane] : 0.0;
+        u = warp_sum(u);
+        if (lane == 0) sh[NW] = u;
     }
-    const double r = sh[0];
     __syncthreads();
+    const double r = sh[NW];
+    __syncthreads();  // sh is reused by the caller's next sum
     return r;
 }
 
