@@ -574,6 +574,17 @@ def run_reference(args):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def flush_c_stdio():
+    """Flush the C stdio buffers of loaded libraries (the compiled reference
+    prints progress with printf), so the JSON line is the last one."""
+    import ctypes
+    try:
+        ctypes.CDLL(None).fflush(None)
+    except (OSError, AttributeError):
+        pass
+    sys.stdout.flush()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -615,7 +626,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)), flush=True)
+            line = run_reference(args)
+            flush_c_stdio()  # the reference's own prints come before the JSON line
+            print(json.dumps(line), flush=True)
         return
     if world > 1:
         import torch
@@ -624,6 +637,7 @@ def main():
         dist.init_process_group("nccl")
     line = run_ours(args, rank, world)
     if rank == 0:
+        flush_c_stdio()
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
