@@ -223,7 +223,7 @@ def run_ours(args, rank, world):
         p.set_model(*init)
         p.set_observed(obs_uz, obs_ux)
         fam, rpt, by = p.autotune() if args.kernels == "auto" else p.shape
-        kernels = {"family": fam, "rows_per_thread": rpt, "block_y": by}
+        kernels = {"family": fam, "rows_per_thread": rpt, "block_y": by, "chains": p.chains}
         stream = torch.cuda.ExternalStream(p.stream)
         flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
 

@@ -61,7 +61,7 @@ class PsvOptions(C.Structure):
         ("checkpoint_interval", C.c_int), ("max_batch", C.c_int), ("use_graphs", C.c_int),
         ("block_x", C.c_int), ("block_y", C.c_int), ("rows_per_thread", C.c_int),
         ("kernel_family", C.c_int), ("autotune", C.c_int), ("checkpoint_slots", C.c_int),
-        ("smooth_hfs", C.c_int), ("pcg", C.c_int),
+        ("smooth_hfs", C.c_int), ("pcg", C.c_int), ("chains", C.c_int),
     ]
 
 
@@ -104,6 +104,7 @@ SIGNATURES = {
     "psv_plan_autotune": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip, _ip]),
     "psv_plan_shape": (C.c_int, [C.c_void_p, _ip, _ip, _ip]),
     "psv_plan_storage": (C.c_int, [C.c_void_p, _ip, _ip, _ip, C.POINTER(C.c_longlong)]),
+    "psv_plan_chains": (C.c_int, [C.c_void_p, _ip]),
     "psv_gauss_filter_kernel": (C.c_int, [C.c_int, _dp]),
     "psv_apply_gauss_filter": (C.c_int, [_dp, C.c_int, C.c_int, C.c_int]),
     "psv_PCG_PSV": (C.c_int, [_dp, _dp, _dp, C.c_int, C.c_int]),

@@ -411,6 +411,13 @@ int psv_plan_autotune(psv_plan *p, int nsteps, int *family, int *rpt, int *by)
     return p->impl->autotune(nsteps, family, rpt, by);
 }
 
+int psv_plan_chains(const psv_plan *p, int *chains)
+{
+    PLAN_CHECK(p);
+    if (chains) *chains = p->impl->chain_count();
+    return PSV_OK;
+}
+
 int psv_plan_storage(const psv_plan *p, int *kind, int *segment_steps, int *slots,
                      long long *advances)
 {

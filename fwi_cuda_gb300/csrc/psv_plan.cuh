@@ -144,6 +144,7 @@ struct PlanIface {
     virtual int autotune(int nsteps, int *fam, int *rpt, int *by) = 0;
     virtual void shape(int *fam, int *rpt, int *by) const = 0;
     virtual void storage(int *kind, int *segment_steps, int *slots, long long *advances) const = 0;
+    virtual int chain_count() const = 0;
     virtual int prepare() = 0;  // history buffers and the pending autotune, before concurrent use
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,

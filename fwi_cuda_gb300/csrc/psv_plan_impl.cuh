@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -21,6 +22,12 @@ using TuneKey = std::tuple<int, int, int, int, int, int>;
 inline std::map<TuneKey, std::tuple<int, int, int>> &tune_cache()
 {
     static std::map<TuneKey, std::tuple<int, int, int>> m;
+    return m;
+}
+// ... and the chain count the autotuner chose for that key.
+inline std::map<TuneKey, int> &chain_cache()
+{
+    static std::map<TuneKey, int> m;
     return m;
 }
 inline std::mutex &tune_mutex()
@@ -89,9 +96,24 @@ public:
     long long nlaunch = 0;          // kernels launched (graph nodes counted per replay)
     long long gx_nodes[NPASS] = {}; // kernels in each captured pass
     dim3 blk{32, 8, 1};
+    // Chained schedule (direct family): the batch split into `chains` groups
+    // of slots whose time loops run on their own (captured) streams, so one
+    // group's launches fill the kernel boundaries of the others.
+    static constexpr int MAXCH = 4;
+    int chains = 1;
+    cudaStream_t stc[MAXCH] = {};
+    cudaEvent_t evf = nullptr, evj[MAXCH] = {};
+    DevMem ctl2;            // [MAXCH][2]: global shot of the group's slot 0, shots
+    int *h_ctl2 = nullptr;  // pinned [nbatch][MAXCH][2]
 
     ~Plan() override
     {
+        if (evf) cudaEventDestroy(evf);
+        for (int k = 0; k < MAXCH; k++) {
+            if (evj[k]) cudaEventDestroy(evj[k]);
+            if (stc[k]) cudaStreamDestroy(stc[k]);
+        }
+        if (h_ctl2) cudaFreeHost(h_ctl2);
         for (auto &g : gx)
             if (g) cudaGraphExecDestroy(g);
         for (auto &e : ev)
@@ -139,6 +161,8 @@ public:
             return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2, 3 or 4");
         if (opt.kernel_family >= PSV_KERNELS_TMA && sizeof(T) != 4)
             return fail(PSV_ERR_UNSUPPORTED, "TMA, VEC4 and FUSED kernels are FP32 only");
+        if (opt.chains != 0 && opt.chains != 1 && opt.chains != 2 && opt.chains != 4)
+            return fail(PSV_ERR_ARG, "chains must be 0 (autotuned), 1, 2 or 4");
         if (opt.smooth_hfs < 0 || opt.smooth_hfs == 1)
             return fail(PSV_ERR_ARG, "smooth_hfs must be 0 (off) or at least 2");
         if (opt.block_y > 0 && opt.block_y <= 8) blk = dim3(32, opt.block_y, 1);
@@ -242,6 +266,13 @@ public:
         for (auto &e : ev) PSV_CU(cudaEventCreate(&e));
         PSV_CU(cudaMallocHost(&h_ctl, sizeof(int) * 2 * nbatch));
         PSV_CU(cudaMallocHost(&h_err, sizeof(int)));
+        PSV_CU(cudaEventCreateWithFlags(&evf, cudaEventDisableTiming));
+        for (int k = 1; k < MAXCH; k++) PSV_CU(cudaStreamCreateWithFlags(&stc[k], cudaStreamNonBlocking));
+        for (int k = 0; k < MAXCH; k++) PSV_CU(cudaEventCreateWithFlags(&evj[k], cudaEventDisableTiming));
+        stc[0] = nullptr;  // chain 0 runs on the plan's stream
+        PSV_CU(cudaMallocHost(&h_ctl2, sizeof(int) * 2 * MAXCH * nbatch));
+        chains = opt.chains == 2 || opt.chains == 4 ? opt.chains : 1;
+        PSV_TRY(set_chains(chains));
         *h_err = 0;
         for (int b = 0; b < nbatch; b++) {
             h_ctl[2 * b] = b * B;
@@ -261,6 +292,8 @@ public:
         PSV_TRY(red.alloc(((size_t)256 * std::max(3, nshot) + nshot + 3 + B + 2) * 8, total));
         PSV_TRY(taperb.alloc((size_t)(nx + nz) * 8, total));
         PSV_TRY(ctl.alloc(4 * sizeof(int), total));
+        PSV_TRY(ctl2.alloc(2 * MAXCH * sizeof(int), total));
+        PSV_CU(cudaMemsetAsync(ctl2.p, 0, 2 * MAXCH * sizeof(int), st));
         PSV_CU(cudaMemsetAsync(ctl.p, 0, 4 * sizeof(int), st));
         PSV_TRY(scales.alloc((size_t)4 * nshot * 8, total));
         {
@@ -317,8 +350,9 @@ public:
 
     // One stress / velocity launch of the current kernel family; `second`
     // selects the checkpoint recompute state.
-    cudaError_t ks(const StepParams<T> &s, bool second)
+    cudaError_t ks(const StepParams<T> &s, bool second, int nb = 0, cudaStream_t sm = nullptr)
     {
+        if (nb) return launch_stress<T>(s, sv.ns, rpt, blk, nb, sm);  // a chain: direct family
         if constexpr (sizeof(T) == 4) {
             if (fam == PSV_KERNELS_TMA)
                 return launch_stress_tma(s, second ? tmap2 : tmap, sv.ns, rpt, B, st);
@@ -328,8 +362,9 @@ public:
         return launch_stress<T>(s, sv.ns, rpt, blk, B, st);
     }
     cudaError_t kv(const StepParams<T> &s, const SrcRecParams<T> &q, int mode, int it, int slot,
-                   bool second)
+                   bool second, int nb = 0, cudaStream_t sm = nullptr)
     {
+        if (nb) return launch_velocity<T>(s, q, sv.ns, mode, it, slot, rpt, blk, nb, sm);
         if constexpr (sizeof(T) == 4) {
             if (fam == PSV_KERNELS_TMA)
                 return launch_velocity_tma(s, q, second ? tmap2 : tmap, sv.ns, mode, it, slot, rpt,
@@ -353,6 +388,59 @@ public:
         return kv(s, q, mode, it, slot, second);
     }
     long long lps() const { return fused() ? 1 : 2; }  // launches per step
+
+    // Parameters of chain k (slots [k h, k h + h), h = ceil(B / chains)):
+    // base pointers moved to the chain's first slot, its own control block.
+    StepParams<T> chain_view(const StepParams<T> &s, int k) const
+    {
+        StepParams<T> v = s;
+        v.ctl = ctl2.as<int>() + 2 * k;
+        const long long o = (long long)k * ((B + chains - 1) / chains);
+        v.fld += o * s.shot_stride;
+        if (v.memz) v.memz += o * s.mz_shot_stride;
+        if (v.memx) v.memx += o * s.mx_shot_stride;
+        if (v.hist) v.hist += o * s.hist_shot_stride;
+        if (v.gshot) v.gshot += o * s.gshot_shot_stride;
+        return v;
+    }
+    int chain_n(int k) const
+    {
+        const int h = (B + chains - 1) / chains;
+        return std::max(0, std::min(h, B - k * h));
+    }
+    // Chains apply to the direct family's full-storage passes (checkpointed
+    // passes interleave recomputation and keep one stream).
+    bool chained() const { return chains > 1 && fam == PSV_KERNELS_DIRECT && !ckpt; }
+    cudaStream_t chain_stream(int k) const { return k ? stc[k] : st; }
+
+    // The time loop of one pass over chains: fork from the plan's stream,
+    // each chain's steps on its stream, join.
+    int enqueue_chained(const SrcRecParams<T> &q, int mode, bool adj, bool store, long long &nk,
+                        int nsteps = -1)
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        const int ns = nsteps < 0 ? nt : nsteps;
+        StepParams<T> v[MAXCH];
+        for (int k = 0; k < chains; k++) v[k] = chain_view(sp, k);
+        PSV_CU(cudaEventRecord(evf, st));
+        for (int k = 1; k < chains; k++) PSV_CU(cudaStreamWaitEvent(stc[k], evf, 0));
+        for (int jt = 0; jt < ns; jt++) {
+            const int it = adj ? nt - 1 - jt : jt;
+            const int slot = (!(it % sdt) && (store || adj)) ? (it / sdt) % sv.snt : -1;
+            for (int k = 0; k < chains; k++) {
+                const int n = chain_n(k);
+                if (n <= 0) continue;
+                PSV_CU(ks(v[k], false, n, chain_stream(k)));
+                PSV_CU(kv(v[k], q, mode, it, slot, false, n, chain_stream(k)));
+                nk += 2;
+            }
+        }
+        for (int k = 1; k < chains; k++) {
+            PSV_CU(cudaEventRecord(evj[k], stc[k]));
+            PSV_CU(cudaStreamWaitEvent(st, evj[k], 0));
+        }
+        return PSV_OK;
+    }
 
     // Wait for the stream, then fail if a time-step kernel gave up a bounded
     // wait (device error word).
@@ -752,6 +840,8 @@ public:
             nk += lps() * nt;
         } else if (ckpt && kind == PASS_ADJ_RES) {
             PSV_TRY(run_schedule(nk));
+        } else if (chained()) {
+            PSV_TRY(enqueue_chained(q, mode, adj, store, nk));
         } else {
             for (int jt = 0; jt < nt; jt++) {
                 const int it = adj ? nt - 1 - jt : jt;
@@ -793,9 +883,29 @@ public:
         return PSV_OK;
     }
 
+    // Group sizes of `k` chains over the batch slots (ceil(B / k) slots each,
+    // the last ones possibly short or empty) and their control blocks.
+    int set_chains(int k)
+    {
+        chains = std::max(1, std::min(k, (int)MAXCH));
+        while (chains > B) chains /= 2;  // 4 -> 2 -> 1: at least one shot a group
+        const int h = (B + chains - 1) / chains;
+        for (int b = 0; b < nbatch; b++) {
+            const int n = std::min(B, sv.s.nshot - b * B);
+            for (int c = 0; c < MAXCH; c++) {
+                h_ctl2[(b * MAXCH + c) * 2] = b * B + c * h;
+                h_ctl2[(b * MAXCH + c) * 2 + 1] = c < chains ? std::max(0, std::min(h, n - c * h)) : 0;
+            }
+        }
+        drop_graphs();
+        return PSV_OK;
+    }
+
     int set_batch(int b)
     {
         PSV_CU(cudaMemcpyAsync(ctl.p, h_ctl + 2 * b, 2 * sizeof(int), cudaMemcpyHostToDevice, st));
+        PSV_CU(cudaMemcpyAsync(ctl2.p, h_ctl2 + 2 * MAXCH * b, 2 * MAXCH * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
         return PSV_OK;
     }
 
@@ -1231,6 +1341,7 @@ public:
             if (it != tune_cache().end()) {
                 PSV_TRY(set_shape(std::get<0>(it->second), std::get<1>(it->second),
                                   std::get<2>(it->second)));
+                if (opt.chains == 0) PSV_TRY(set_chains(chain_cache()[key]));
                 tuned = true;
                 report();
                 return PSV_OK;
@@ -1263,14 +1374,28 @@ public:
             if (t < best) { best = t; pick = {fam, rpt, (int)blk.y}; }
         }
         PSV_TRY(set_shape(std::get<0>(pick), std::get<1>(pick), std::get<2>(pick)));
+        int ck = chains;
+        if (opt.chains == 0 && fam == PSV_KERNELS_DIRECT && B >= 2 && !ckpt) {
+            double tb = 1e30;
+            for (int k : {1, 2, 4}) {
+                if (k > B) continue;
+                double t = 0;
+                PSV_TRY(time_chains(nsteps, k, &t));
+                if (t < tb) { tb = t; ck = k; }
+            }
+        }
+        PSV_TRY(set_chains(ck));
         {
             std::lock_guard<std::mutex> lk(tune_mutex());
             tune_cache()[key] = pick;
+            chain_cache()[key] = ck;
         }
         tuned = true;
         report();
         return PSV_OK;
     }
+
+    int chain_count() const override { return chained() ? chains : 1; }
 
     void storage(int *kind, int *segment_steps, int *slots, long long *advances) const override
     {
@@ -1304,6 +1429,70 @@ public:
     long long launches() const override { return nlaunch; }
 
     // Per-kernel event timing of nsteps forward then nsteps adjoint steps.
+    // Device milliseconds of nsteps forward + nsteps adjoint steps of the
+    // current shape with k chains (the autotuner's chain choice), replayed
+    // as a CUDA graph like the passes themselves (direct launches would time
+    // the host's launch rate instead).
+    int time_chains(int nsteps, int k, double *ms)
+    {
+        PSV_TRY(set_chains(k));
+        PSV_TRY(set_batch(0));
+        T *f = fld.as<T>();
+        PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, shot_stride, B, st));
+        PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+        PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+        PSV_CU(cudaStreamSynchronize(st));
+        long long nk = 0;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        PSV_CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int rc = burst(nsteps, nk);
+        const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (rc != PSV_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(PSV_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return fail(PSV_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        cudaError_t e = cudaGraphLaunch(exec, st);  // warm-up
+        if (e == cudaSuccess) e = cudaEventRecord(ev[0], st);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, st);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaGraphExecDestroy(exec);
+        if (e != cudaSuccess) return fail(PSV_ERR_CUDA, cudaGetErrorString(e));
+        PSV_TRY(sync_check());
+        float t = 0;
+        PSV_CU(cudaEventElapsedTime(&t, ev[0], ev[1]));
+        *ms = t;
+        nlaunch += 2 * nk;
+        return PSV_OK;
+    }
+
+    // nsteps forward and nsteps adjoint steps of the current schedule.
+    int burst(int nsteps, long long &nk)
+    {
+        for (int pass = 0; pass < 2; pass++) {
+            const bool adj = pass == 1;
+            const SrcRecParams<T> &q = adj ? qa : qf;
+            const int mode = adj ? MODE_ADJ : MODE_FWD;
+            if (chained()) {
+                PSV_TRY(enqueue_chained(q, mode, adj, true, nk, nsteps));
+            } else {
+                const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+                for (int j = 0; j < nsteps; j++) {
+                    const int it = adj ? nt - 1 - j : j;
+                    const int slot = !(it % sdt) ? (it / sdt) % (ckpt ? nslots : sv.snt) : -1;
+                    PSV_CU(step(sp, q, mode, it, slot, false, par(j)));
+                    nk += lps();
+                }
+            }
+        }
+        return PSV_OK;
+    }
+
     int profile(int nsteps, double *ms6) override
     {
         if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "profile: model and observed traces required");

@@ -25,7 +25,7 @@ FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused"}
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
             block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
-            kernels="any", checkpoint_slots=0, smooth_hfs=0, pcg=False) -> PsvOptions:
+            kernels="any", checkpoint_slots=0, smooth_hfs=0, pcg=False, chains=0) -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -38,6 +38,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.checkpoint_slots = int(checkpoint_slots)
     o.smooth_hfs = int(smooth_hfs)
     o.pcg = int(bool(pcg))
+    o.chains = int(chains)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
     o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4}[kernels]
@@ -220,6 +221,13 @@ class Plan:
         f, r, b = C.c_int(), C.c_int(), C.c_int()
         check(_lib.lib().psv_plan_shape(self.h, C.byref(f), C.byref(r), C.byref(b)))
         return FAMILIES[f.value], r.value, b.value
+
+    @property
+    def chains(self):
+        """Shot groups (streams) the time loops run in."""
+        c = C.c_int()
+        check(_lib.lib().psv_plan_chains(self.h, C.byref(c)))
+        return c.value
 
     @property
     def storage(self):

@@ -153,6 +153,10 @@ typedef struct psv_options {
     int pcg;                    /* 1: psv_fwi_iteration turns the global gradients into
                                    Fletcher-Reeves directions before the taper (the
                                    reference's commented-out PCG_PSV calls, :433-435) */
+    int chains;                 /* direct family with full storage: the batch's shots split
+                                   into 1, 2 or 4 groups whose time loops run on their own
+                                   streams (each group's launches fill the others' kernel
+                                   boundaries); 0 = the autotuner picks */
 } psv_options;
 
 void psv_options_default(psv_options *opt);
@@ -330,6 +334,8 @@ int psv_plan_autotune(psv_plan *plan, int nsteps, int *kernel_family, int *rows_
  * per thread (FUSED: tile rows) and block height (TMA: 4, FUSED: 0); any
  * pointer may be NULL. */
 int psv_plan_shape(const psv_plan *plan, int *kernel_family, int *rows_per_thread, int *block_y);
+/* Shot groups (streams) the plan's time loops run in: 1, 2 or 4. */
+int psv_plan_chains(const psv_plan *plan, int *chains);
 /* The plan's snapshot storage: PSV_STORE_FULL, _CHECKPOINT or _BINOMIAL
  * (never AUTO), steps per segment and state slots per shot (0 for FULL),
  * and the segment advances the adjoint pass recomputes beyond the one

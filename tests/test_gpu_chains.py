@@ -1,0 +1,60 @@
+"""Chained time loops: the batch's shots split into groups whose launches run
+on their own streams.  Each shot's arithmetic is unchanged, so gradients,
+traces and misfits equal the single-stream schedule bit for bit."""
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import _lib, engine
+
+pytestmark = pytest.mark.gpu
+
+SHAPE = dict(precision=32, kernels="direct", rows_per_thread=1, block=(32, 4))
+
+
+def _run(sv, init, uz, ux, **opt):
+    with engine.Plan(sv, **dict(SHAPE, **opt)) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L2, g = p.gradient()
+        fwd = p.forward()
+        return p.chains, L2, g, fwd
+
+
+@pytest.mark.parametrize("nshot,max_batch,chains", [(8, 0, 2), (8, 0, 4), (5, 0, 2), (5, 0, 4),
+                                                     (7, 3, 2), (7, 3, 4)])
+def test_chains_equal_one_stream(gpu, orc, nshot, max_batch, chains):
+    # 5 shots in 4 groups: ceil(5 / 4) = 2 slots a group, the last group empty;
+    # 7 shots in batches of 3: the last batch holds one shot
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=nshot, nt=200, snap_dt=2)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    c1, L1, g1, f1 = _run(sv, init, uz, ux, max_batch=max_batch, chains=1)
+    c2, L2, g2, f2 = _run(sv, init, uz, ux, max_batch=max_batch, chains=chains)
+    assert c1 == 1 and c2 == (chains if chains <= (max_batch or nshot) else 2)
+    assert L1 == L2
+    for a, b in zip(g1 + list(f1), g2 + list(f2)):
+        assert np.array_equal(a, b)
+
+
+def test_checkpointed_plans_ignore_chains(gpu, orc):
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=4, nt=200, snap_dt=2)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    _, L1, g1, _ = _run(sv, init, uz, ux, storage="checkpoint", chains=1)
+    _, L2, g2, _ = _run(sv, init, uz, ux, storage="checkpoint", chains=4)
+    assert L1 == L2 and all(np.array_equal(a, b) for a, b in zip(g1, g2))
+
+
+def test_autotuner_picks_a_chain_count(gpu, orc):
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=4, nt=100)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    with engine.Plan(sv, precision=32, kernels="direct") as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        p.autotune(8)
+        assert p.chains in (1, 2, 4)
+
+
+def test_bad_chain_count_is_rejected(gpu):
+    sv, _, _ = helpers.case(nshot=2, nt=20)
+    with pytest.raises(_lib.PSVError, match="chains"):
+        engine.Plan(sv, precision=32, chains=3)
