@@ -320,6 +320,9 @@ def run_ours(args, rank, world):
         "config": config_dict(world, {"kernels": kernels}),
         "shots_per_s": nshot * world / (ms / 1e3),
         "split_ms": {k: round(v, 3) for k, v in split.items()},
+        # forward-only and adjoint-only rates of the same gradient (device time)
+        "updates_per_s_forward": nshot * world * nt * CFG["nz"] * CFG["nx"] / (split["forward_ms"] * 1e-3),
+        "updates_per_s_adjoint": nshot * world * nt * CFG["nz"] * CFG["nx"] / (split["adjoint_ms"] * 1e-3),
         "e2e": {"value": updates_per_step(nt, nshot) * world / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
@@ -436,6 +439,7 @@ def large_grid(args):
         t0 = time.perf_counter()
         p.gradient(fetch=False)
         sec = time.perf_counter() - t0
+        tm = p.timing()
         prof = p.profile_kernels(nsteps=100)
     pts = c["nz"] * c["nx"] * c["nshot"]
     peak, src = peaks()
@@ -448,6 +452,8 @@ def large_grid(args):
                         "FP32, snap_dt=3", "kernels": {"family": fam, "rows_per_thread": rpt,
                                                         "block_y": by},
             "updates_per_s": 2.0 * pts * c["nt"] / sec, "gradient_s": sec,
+            "updates_per_s_forward": pts * c["nt"] / (tm["forward_ms"] * 1e-3),
+            "updates_per_s_adjoint": pts * c["nt"] / (tm["adjoint_ms"] * 1e-3),
             "peak_gbs": peak, "peak_source": src, "per_kernel": kern}
 
 
