@@ -2,6 +2,7 @@
 // Instantiated for float (psv_plan_f32.cu) and double (psv_plan_f64.cu).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -1366,24 +1367,34 @@ public:
                 if (fused_ok(tz)) cand.emplace_back(PSV_KERNELS_FUSED, tz, (int)blk.y);
         double best = 1e30;
         std::tuple<int, int, int> pick{fam, rpt, (int)blk.y};
+        std::vector<std::pair<double, std::tuple<int, int, int>>> direct;
         for (auto &c : cand) {
             PSV_TRY(set_shape(std::get<0>(c), std::get<1>(c), std::get<2>(c)));
             double ms[6];
             PSV_TRY(profile(nsteps, ms));
             const double t = ms[0] + ms[1] + ms[3] + ms[4];
             if (t < best) { best = t; pick = {fam, rpt, (int)blk.y}; }
+            if (fam == PSV_KERNELS_DIRECT) direct.emplace_back(t, std::make_tuple(fam, rpt, (int)blk.y));
         }
-        PSV_TRY(set_shape(std::get<0>(pick), std::get<1>(pick), std::get<2>(pick)));
         int ck = chains;
-        if (opt.chains == 0 && fam == PSV_KERNELS_DIRECT && B >= 2 && !ckpt) {
+        if (opt.chains == 0 && std::get<0>(pick) == PSV_KERNELS_DIRECT && B >= 2 && !ckpt) {
+            // the three fastest direct shapes again, with 1, 2 and 4 chains,
+            // as graph-replayed bursts: chaining can reorder them
+            std::sort(direct.begin(), direct.end(),
+                      [](const auto &a, const auto &b) { return a.first < b.first; });
             double tb = 1e30;
-            for (int k : {1, 2, 4}) {
-                if (k > B) continue;
-                double t = 0;
-                PSV_TRY(time_chains(nsteps, k, &t));
-                if (t < tb) { tb = t; ck = k; }
+            for (size_t i = 0; i < std::min<size_t>(3, direct.size()); i++) {
+                const auto &sh = direct[i].second;
+                PSV_TRY(set_shape(std::get<0>(sh), std::get<1>(sh), std::get<2>(sh)));
+                for (int k : {1, 2, 4}) {
+                    if (k > B) continue;
+                    double t = 0;
+                    PSV_TRY(time_chains(nsteps, k, &t));
+                    if (t < tb) { tb = t; ck = k; pick = sh; }
+                }
             }
         }
+        PSV_TRY(set_shape(std::get<0>(pick), std::get<1>(pick), std::get<2>(pick)));
         PSV_TRY(set_chains(ck));
         {
             std::lock_guard<std::mutex> lk(tune_mutex());
