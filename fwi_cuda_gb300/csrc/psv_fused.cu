@@ -23,8 +23,6 @@
 // Free surface: only a top surface (the rows above it mirror the rows
 // below, within the first tile row's stress region); bottom, left and right
 // surfaces use the two-launch families (fused_supported).
-#include <mutex>
-
 #include "psv_kernels_impl.cuh"
 #include "psv_plan.cuh"
 
