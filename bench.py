@@ -299,6 +299,7 @@ def run_ours(args, rank, world):
             fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
     large = large_grid(args) if rank == 0 and not args.no_large else None
     uneven = uneven_batch(args) if rank == 0 and not args.no_uneven else None
+    small = small_surveys(args) if rank == 0 and not args.no_uneven else None
     batching = None
     if rank == 0 and not args.no_batching:
         shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by))
@@ -342,6 +343,8 @@ def run_ours(args, rank, world):
         line["large_grid"] = large
     if uneven:
         line["uneven_batch"] = uneven
+    if small:
+        line["small_surveys"] = small
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
     return line
@@ -500,6 +503,52 @@ def uneven_batch(args):
             p.close()
 
 
+def small_surveys(args):
+    """Eight small surveys (101 x 201, 2 shots, nt 500, order 4, one model
+    each): one FWI gradient of all eight through psv_multi_gradient (one
+    stream per survey), one after another, and one survey holding all 16
+    shots (one launch per half-step: the most a single launch over the eight
+    surveys could reach)."""
+    from fwi_cuda_gb300 import engine, survey as S
+    plans = []
+
+    def plan(nshot, seed):
+        sv, true, init = S.config_layered(nz=101, nx=201, dx=0.5, nt=500, dt=5e-5, nshot=nshot,
+                                          fdorder=4, npml=10, nrec=40, snap_dt=3, seed=seed,
+                                          surf_offset=0)
+        p = engine.Plan(sv, precision=32, **plan_kernels(args))
+        plans.append(p)
+        p.set_model(*true)
+        obs = p.forward()
+        p.set_model(*init)
+        p.set_observed(*obs)
+        return p
+
+    try:
+        each = [plan(2, 200 + k) for k in range(8)]
+        joint = plan(16, 300)
+        engine.multi_gradient(each)  # tunes and captures graphs
+        joint.gradient(fetch=False)
+        t0 = time.perf_counter()
+        engine.multi_gradient(each)
+        conc = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for p in each:
+            p.gradient(fetch=False)
+        seq = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        joint.gradient(fetch=False)
+        one = time.perf_counter() - t0
+        upd = 2.0 * 16 * 500 * 101 * 201
+        return {"workload": "8 surveys of 101x201, 2 shots each, nt 500, order 4, FP32",
+                "concurrent_s": conc, "sequential_s": seq, "one_survey_16_shots_s": one,
+                "concurrent_updates_per_s": upd / conc, "sequential_updates_per_s": upd / seq,
+                "one_survey_updates_per_s": upd / one}
+    finally:
+        for p in plans:
+            p.close()
+
+
 FULL = {  # the batched-survey and the large single-model configurations
     "c3": dict(nz=1001, nx=2001, dx=0.5, dt=2.5e-5, nt=10000, nshot=64, nrec=500, rec_spacing=3,
                fdorder=8, npml=30, layers=8, dip=60.0, fault=None, anomalies=6, radius=(10, 30),
@@ -605,7 +654,7 @@ def main():
     ap.add_argument("--slots", type=int, default=0,
                     help="state slots per shot with --storage binomial (0 = the library's choice)")
     ap.add_argument("--no-uneven", action="store_true",
-                    help="skip the four-survey uneven-batch leg")
+                    help="skip the multi-survey legs (uneven grids, small surveys)")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 1001x2001 per-kernel bandwidth leg")
     ap.add_argument("--no-batching", action="store_true",
