@@ -58,3 +58,21 @@ def test_bad_chain_count_is_rejected(gpu):
     sv, _, _ = helpers.case(nshot=2, nt=20)
     with pytest.raises(_lib.PSVError, match="chains"):
         engine.Plan(sv, precision=32, chains=3)
+
+
+def test_fwi_iterations_do_not_depend_on_chains(gpu, orc):
+    # gradient, taper, the step-length search's trial forwards and the update
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=4, nt=250)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    out = []
+    for chains in (1, 4):
+        with engine.Plan(sv, **dict(SHAPE, chains=chains)) as p:
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            steps = [p.fwi_iteration(0.01) for _ in range(2)]
+            out.append((steps, p.get_model()))
+    (s1, m1), (s2, m2) = out
+    for a, b in zip(s1, s2):
+        assert a["step"] == b["step"] and a["L2"] == b["L2"] and a["ntrials"] == b["ntrials"]
+    for a, b in zip(m1, m2):
+        assert np.array_equal(a, b)
