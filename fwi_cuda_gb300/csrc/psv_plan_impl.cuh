@@ -1365,32 +1365,35 @@ public:
         if (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_FUSED)
             for (int tz : {16, 32})
                 if (fused_ok(tz)) cand.emplace_back(PSV_KERNELS_FUSED, tz, (int)blk.y);
-        double best = 1e30;
-        std::tuple<int, int, int> pick{fam, rpt, (int)blk.y};
-        std::vector<std::pair<double, std::tuple<int, int, int>>> direct;
+        // 1) every candidate, launch by launch with CUDA events
+        std::vector<std::pair<double, std::tuple<int, int, int>>> timed;
         for (auto &c : cand) {
             PSV_TRY(set_shape(std::get<0>(c), std::get<1>(c), std::get<2>(c)));
             double ms[6];
             PSV_TRY(profile(nsteps, ms));
-            const double t = ms[0] + ms[1] + ms[3] + ms[4];
-            if (t < best) { best = t; pick = {fam, rpt, (int)blk.y}; }
-            if (fam == PSV_KERNELS_DIRECT) direct.emplace_back(t, std::make_tuple(fam, rpt, (int)blk.y));
+            timed.emplace_back(ms[0] + ms[1] + ms[3] + ms[4], std::make_tuple(fam, rpt, (int)blk.y));
         }
+        std::sort(timed.begin(), timed.end(),
+                  [](const auto &a, const auto &b) { return a.first < b.first; });
+        // 2) the three fastest again as graph-replayed bursts of forward +
+        // adjoint steps, the way the passes run, with 1, 2 and 4 chains for
+        // the direct family (chaining can reorder them)
+        std::tuple<int, int, int> pick = timed.empty() ? std::make_tuple(fam, rpt, (int)blk.y)
+                                                       : timed.front().second;
         int ck = chains;
-        if (opt.chains == 0 && std::get<0>(pick) == PSV_KERNELS_DIRECT && B >= 2 && !ckpt) {
-            // the three fastest direct shapes again, with 1, 2 and 4 chains,
-            // as graph-replayed bursts: chaining can reorder them
-            std::sort(direct.begin(), direct.end(),
-                      [](const auto &a, const auto &b) { return a.first < b.first; });
-            double tb = 1e30;
-            for (size_t i = 0; i < std::min<size_t>(3, direct.size()); i++) {
-                const auto &sh = direct[i].second;
-                PSV_TRY(set_shape(std::get<0>(sh), std::get<1>(sh), std::get<2>(sh)));
-                for (int k : {1, 2, 4}) {
-                    if (k > B) continue;
-                    double t = 0;
-                    PSV_TRY(time_chains(nsteps, k, &t));
-                    if (t < tb) { tb = t; ck = k; pick = sh; }
+        double tb = 1e30;
+        for (size_t i = 0; i < std::min<size_t>(3, timed.size()); i++) {
+            const auto &sh = timed[i].second;
+            PSV_TRY(set_shape(std::get<0>(sh), std::get<1>(sh), std::get<2>(sh)));
+            const bool chainable = opt.chains == 0 && fam == PSV_KERNELS_DIRECT && B >= 2 && !ckpt;
+            for (int k : {1, 2, 4}) {
+                if (chainable ? k > B : k != 1) continue;
+                double t = 0;
+                PSV_TRY(time_chains(nsteps, chainable ? k : chains, &t));
+                if (t < tb) {
+                    tb = t;
+                    pick = sh;
+                    ck = chainable ? k : chains;
                 }
             }
         }
