@@ -198,3 +198,39 @@ def test_misfit_entry_point_matches_oracle(gpu, orc):
         L2o, az, ax = orc.adjsrc2(mod[s], modx[s], obs[s], obsx[s], 5e-5)
         assert L2[s] == pytest.approx(L2o, rel=1e-13)
         assert np.array_equal(rz[s], az) and np.array_equal(rx[s], ax)
+
+
+def test_survey_without_receivers(gpu, orc):
+    # no receivers: forward modelling runs (empty traces); observed data, and
+    # so a gradient, is refused with an error status instead of a zero misfit
+    from fwi_cuda_gb300 import _lib
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=120)
+    sv.z_rec = np.zeros(0, np.int32)
+    sv.x_rec = np.zeros(0, np.int32)
+    sv.finalize()
+    for precision in (32, 64):
+        with engine.Plan(sv, precision=precision) as p:
+            p.set_model(*true)
+            uz, ux = p.forward()
+            assert uz.shape == (2, 0, sv.nt) and ux.shape == (2, 0, sv.nt)
+            with pytest.raises(_lib.PSVError, match="no receivers"):
+                p.set_observed(uz, ux)
+            with pytest.raises(_lib.PSVError):
+                p.gradient()
+
+
+def test_single_shot_with_chains_requested(gpu, orc):
+    # one shot a batch: nothing to split, the plan runs one stream
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=1, nt=150)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    out = []
+    for chains in (1, 4):
+        with engine.Plan(sv, precision=32, kernels="direct", rows_per_thread=1, block=(32, 4),
+                         chains=chains) as p:
+            assert p.chains == 1
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            out.append(p.gradient())
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
