@@ -140,9 +140,10 @@ typedef struct psv_options {
     int kernel_family;          /* time-step kernels: 0 = any (the autotuner chooses),
                                    PSV_KERNELS_DIRECT, _TMA, _VEC4 or _FUSED (the last three
                                    FP32 only; FUSED needs no free surface but a top one) */
-    int autotune;               /* 1 (default): time the tile-shape candidates on the first
-                                   time loop and keep the fastest (psv_plan_autotune);
-                                   0: use block_y / rows_per_thread as given */
+    int autotune;               /* 1 (default): time the kernel candidates (family, tile
+                                   shape and, for the direct family, the chain count) on the
+                                   first gradient and keep the fastest (psv_plan_autotune);
+                                   0: use block_y / rows_per_thread / chains as given */
     int checkpoint_slots;       /* BINOMIAL storage: state slots per shot (segment 0's
                                    included); 0 = the fewest with at most two forward
                                    repetitions, fewer if the budget holds fewer */
