@@ -302,7 +302,7 @@ def run_ours(args, rank, world):
     small = small_surveys(args) if rank == 0 and not args.no_uneven else None
     batching = None
     if rank == 0 and not args.no_batching:
-        shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by))
+        shape = dict(kernels=fam, rows_per_thread=rpt, block=(32, by), chains=kernels["chains"])
         batching = batching_compare(sv, init, obs_uz, obs_ux, shape, nshot / (ms / 1e3))
 
     if rank != 0:

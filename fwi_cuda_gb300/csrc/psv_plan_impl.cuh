@@ -409,30 +409,31 @@ public:
         const int h = (B + chains - 1) / chains;
         return std::max(0, std::min(h, B - k * h));
     }
-    // Chains apply to the direct family's full-storage passes (checkpointed
-    // passes interleave recomputation and keep one stream).
-    bool chained() const { return chains > 1 && fam == PSV_KERNELS_DIRECT && !ckpt; }
+    // Chains apply to the direct family's passes; checkpointed passes join
+    // them around every copy of the batch's states.
+    bool chained() const { return chains > 1 && fam == PSV_KERNELS_DIRECT; }
     cudaStream_t chain_stream(int k) const { return k ? stc[k] : st; }
 
     // The time loop of one pass over chains: fork from the plan's stream,
     // each chain's steps on its stream, join.
-    int enqueue_chained(const SrcRecParams<T> &q, int mode, bool adj, bool store, long long &nk,
-                        int nsteps = -1)
+    // Steps it of state s over the chains (fork from the plan's stream, each
+    // group's steps on its stream, join): its[j] for j < nstep, snapshot slot
+    // slot_of(it).
+    template <typename ItFn, typename SlotFn>
+    int chained_steps(const StepParams<T> &s, const SrcRecParams<T> &q, int mode, int nstep,
+                      ItFn it_of, SlotFn slot_of, bool second, long long &nk)
     {
-        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
-        const int ns = nsteps < 0 ? nt : nsteps;
         StepParams<T> v[MAXCH];
-        for (int k = 0; k < chains; k++) v[k] = chain_view(sp, k);
+        for (int k = 0; k < chains; k++) v[k] = chain_view(s, k);
         PSV_CU(cudaEventRecord(evf, st));
         for (int k = 1; k < chains; k++) PSV_CU(cudaStreamWaitEvent(stc[k], evf, 0));
-        for (int jt = 0; jt < ns; jt++) {
-            const int it = adj ? nt - 1 - jt : jt;
-            const int slot = (!(it % sdt) && (store || adj)) ? (it / sdt) % sv.snt : -1;
+        for (int j = 0; j < nstep; j++) {
+            const int it = it_of(j), slot = slot_of(it);
             for (int k = 0; k < chains; k++) {
                 const int n = chain_n(k);
                 if (n <= 0) continue;
-                PSV_CU(ks(v[k], false, n, chain_stream(k)));
-                PSV_CU(kv(v[k], q, mode, it, slot, false, n, chain_stream(k)));
+                PSV_CU(ks(v[k], second, n, chain_stream(k)));
+                PSV_CU(kv(v[k], q, mode, it, slot, second, n, chain_stream(k)));
                 nk += 2;
             }
         }
@@ -441,6 +442,16 @@ public:
             PSV_CU(cudaStreamWaitEvent(st, evj[k], 0));
         }
         return PSV_OK;
+    }
+
+    int enqueue_chained(const SrcRecParams<T> &q, int mode, bool adj, bool store, long long &nk,
+                        int nsteps = -1)
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt, ring = ckpt ? nslots : sv.snt;
+        return chained_steps(
+            sp, q, mode, nsteps < 0 ? nt : nsteps, [&](int j) { return adj ? nt - 1 - j : j; },
+            [&](int it) { return (!(it % sdt) && (store || adj)) ? (it / sdt) % ring : -1; }, false,
+            nk);
     }
 
     // Wait for the stream, then fail if a time-step kernel gave up a bounded
@@ -771,10 +782,23 @@ public:
             // forward pass); adjoint step it is step nt - 1 - it of its pass
             if (x.op == CK_RESTORE || x.op == CK_SAVE_WORK) {
                 PSV_TRY(ck_copy(x.slot, x.op, par(a)));
+            } else if (x.op == CK_ADVANCE && chained()) {
+                PSV_TRY(chained_steps(
+                    sp2, qr, MODE_FWD_NOWE, e - a, [&](int j) { return a + j; },
+                    [](int) { return -1; }, true, nk));
             } else if (x.op == CK_ADVANCE) {
                 for (int it = a; it < e; it++)
                     PSV_CU(step(sp2, qr, MODE_FWD_NOWE, it, -1, true, par(it)));
                 nk += lps() * (e - a);
+            } else if (x.op == CK_REVERSE && chained()) {
+                const int base = (a + sdt - 1) / sdt, last = (e - 1) / sdt * sdt;
+                auto slot_of = [&](int it) { return !(it % sdt) ? it / sdt - base : -1; };
+                PSV_TRY(chained_steps(
+                    sp2, qr, MODE_FWD_NOWE, std::max(last - a + 1, 0),
+                    [&](int j) { return a + j; }, slot_of, true, nk));
+                PSV_TRY(chained_steps(
+                    sp, qa, MODE_ADJ, e - a, [&](int j) { return e - 1 - j; }, slot_of, false,
+                    nk));
             } else if (x.op == CK_REVERSE) {
                 // recompute up to the segment's last snapshot step into the
                 // segment buffer, then the segment's adjoint steps
@@ -831,7 +855,16 @@ public:
         PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
         long long nk = (mode == MODE_ADJ ? 5 : mode == MODE_FWD ? 4 : 3);
-        if (ckpt && kind == PASS_FWD_STORE) {
+        if (ckpt && kind == PASS_FWD_STORE && chained()) {
+            // one segment at a time: its state saved, then its steps on the chains
+            for (int a = 0; a < nt; a += K) {
+                if (fwd_slot[(size_t)(a / K)] >= 0)
+                    PSV_TRY(ck_copy(fwd_slot[(size_t)(a / K)], CK_SAVE_MAIN, par(a)));
+                PSV_TRY(chained_steps(
+                    sp, qf, mode, std::min(K, nt - a), [&](int j) { return a + j; },
+                    [](int) { return -1; }, false, nk));
+            }
+        } else if (ckpt && kind == PASS_FWD_STORE) {
             // forward saving the schedule's states at the starts of their segments
             for (int it = 0; it < nt; it++) {
                 if (!(it % K) && fwd_slot[(size_t)(it / K)] >= 0)
@@ -1385,7 +1418,7 @@ public:
         for (size_t i = 0; i < std::min<size_t>(3, timed.size()); i++) {
             const auto &sh = timed[i].second;
             PSV_TRY(set_shape(std::get<0>(sh), std::get<1>(sh), std::get<2>(sh)));
-            const bool chainable = opt.chains == 0 && fam == PSV_KERNELS_DIRECT && B >= 2 && !ckpt;
+            const bool chainable = opt.chains == 0 && fam == PSV_KERNELS_DIRECT && B >= 2;
             for (int k : {1, 2, 4}) {
                 if (chainable ? k > B : k != 1) continue;
                 double t = 0;

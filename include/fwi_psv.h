@@ -154,10 +154,11 @@ typedef struct psv_options {
     int pcg;                    /* 1: psv_fwi_iteration turns the global gradients into
                                    Fletcher-Reeves directions before the taper (the
                                    reference's commented-out PCG_PSV calls, :433-435) */
-    int chains;                 /* direct family with full storage: the batch's shots split
-                                   into 1, 2 or 4 groups whose time loops run on their own
-                                   streams (each group's launches fill the others' kernel
-                                   boundaries); 0 = the autotuner picks */
+    int chains;                 /* direct family: the batch's shots split into 1, 2 or 4
+                                   groups whose time loops run on their own streams (each
+                                   group's launches fill the others' kernel boundaries;
+                                   checkpointed passes join them around every state copy);
+                                   0 = the autotuner picks */
 } psv_options;
 
 void psv_options_default(psv_options *opt);

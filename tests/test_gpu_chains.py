@@ -36,12 +36,22 @@ def test_chains_equal_one_stream(gpu, orc, nshot, max_batch, chains):
         assert np.array_equal(a, b)
 
 
-def test_checkpointed_plans_ignore_chains(gpu, orc):
+@pytest.mark.parametrize("storage,kw", [("checkpoint", dict(checkpoint_interval=37)),
+                                        ("binomial", dict(checkpoint_slots=3))])
+def test_checkpointed_chains_equal_one_stream(gpu, orc, storage, kw):
+    # the forward saves states between chained segments; the adjoint's
+    # recomputations and reversals run chained between the state copies
     sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=4, nt=200, snap_dt=2)
     uz, ux = orc.simulate_fwd(sv, *true)
-    _, L1, g1, _ = _run(sv, init, uz, ux, storage="checkpoint", chains=1)
-    _, L2, g2, _ = _run(sv, init, uz, ux, storage="checkpoint", chains=4)
+    c1, L1, g1, _ = _run(sv, init, uz, ux, storage=storage, chains=1, **kw)
+    c2, L2, g2, _ = _run(sv, init, uz, ux, storage=storage, chains=4, **kw)
+    assert c1 == 1 and c2 == 4
     assert L1 == L2 and all(np.array_equal(a, b) for a, b in zip(g1, g2))
+    with engine.Plan(sv, **dict(SHAPE, storage="full")) as p:
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L0, g0 = p.gradient()
+    assert L0 == L1 and all(np.array_equal(a, b) for a, b in zip(g0, g1))
 
 
 def test_autotuner_picks_a_chain_count(gpu, orc):
