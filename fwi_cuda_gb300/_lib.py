@@ -17,6 +17,7 @@ _ip = C.POINTER(C.c_int)
 
 PSV_OK, PSV_ERR_ARG, PSV_ERR_CFL, PSV_ERR_OOM, PSV_ERR_CUDA = 0, 1, 2, 3, 4
 PSV_ERR_UNSUPPORTED, PSV_ERR_TIMEOUT, PSV_ERR_STEP_SEARCH, PSV_ERR_IO = 5, 6, 7, 8
+PSV_MAX_NZ, PSV_MAX_SHOTS, PSV_MAX_SHOT_ELEMS = 65535, 65535, 2**31 - 1
 STENCIL = {"reference": 0, "holberg": 1}
 STORAGE = {"auto": 0, "full": 1, "checkpoint": 2, "binomial": 3}
 

@@ -45,6 +45,8 @@ int make_survey(const psv_grid *gp, const psv_shots *sp, Survey &out)
     sv.g = *gp;
     psv_grid &g = sv.g;
     if (g.nt <= 0 || g.nz <= 0 || g.nx <= 0) return fail(PSV_ERR_ARG, "nt, nz, nx must be positive");
+    // Blocks of grid rows map to gridDim.y, which holds at most 65535.
+    if (g.nz > PSV_MAX_NZ) return fail(PSV_ERR_UNSUPPORTED, "nz above 65535");
     if (!(g.dt > 0) || !(g.dx > 0) || !(g.dz > 0)) return fail(PSV_ERR_ARG, "dt, dx, dz must be positive");
     if (g.fdorder != 2 && g.fdorder != 4 && g.fdorder != 6 && g.fdorder != 8)
         return fail(PSV_ERR_UNSUPPORTED, "fdorder must be 2, 4, 6 or 8");
@@ -110,6 +112,8 @@ int make_survey(const psv_grid *gp, const psv_shots *sp, Survey &out)
     sv.s = *sp;
     const psv_shots &s = *sp;
     if (s.nshot <= 0 || s.nsrc < 0 || s.nrec < 0) return fail(PSV_ERR_ARG, "nshot must be > 0, nsrc/nrec >= 0");
+    // The shots of a batch and of the misfit map to gridDim.y / gridDim.z.
+    if (s.nshot > PSV_MAX_SHOTS) return fail(PSV_ERR_UNSUPPORTED, "nshot above 65535");
     if (s.stf_type != 0 && s.stf_type != 1) return fail(PSV_ERR_ARG, "stf_type must be 0 or 1");
     if (s.nsrc && (!s.z_src || !s.x_src || !s.src_shot_to_fire || !s.stf_z || !s.stf_x))
         return fail(PSV_ERR_ARG, "source arrays missing");

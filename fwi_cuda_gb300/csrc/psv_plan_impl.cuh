@@ -188,6 +188,12 @@ public:
         pitch = round_up(nx, al);
         plane = (long long)nz * pitch;
         shot_stride = (long long)nfield() * plane;
+        // The time-step kernels address one shot's field planes with 32-bit
+        // offsets.
+        if (shot_stride > PSV_MAX_SHOT_ELEMS)
+            return fail(PSV_ERR_UNSUPPORTED, "grid too large: one shot's field planes exceed "
+                                             "2^31 - 1 elements (nz x padded nx x " +
+                                                 std::to_string(nfield()) + " planes)");
         nzs = g.pml_z ? sv.pz0 + (nz - sv.pz1) : 0;
         nxs = g.pml_x ? sv.px0 + (nx - sv.px1) : 0;
         mx_pitch = nxs ? round_up(nxs, al) : 0;

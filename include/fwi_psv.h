@@ -57,6 +57,15 @@ typedef enum {
 #define PSV_KERNELS_FUSED 4     /* one launch per time step: stress of a tile and its halo,
                                    then its velocities, from shared memory (FP32) */
 
+/* Size limits (PSV_ERR_UNSUPPORTED above them).  The reference has none
+ * besides memory; here grid rows and shots map to CUDA grid dimensions and
+ * the time-step kernels address one shot's field planes with 32-bit offsets:
+ * nz x (nx padded to 128 bytes) x planes, 14 planes in FP32 (the second
+ * velocity / stress copy of the FUSED family included), 9 in FP64. */
+#define PSV_MAX_NZ 65535
+#define PSV_MAX_SHOTS 65535
+#define PSV_MAX_SHOT_ELEMS 2147483647LL
+
 const char *psv_error_string(int status);
 /* Message of the last failing call on this host thread. */
 const char *psv_last_error(void);

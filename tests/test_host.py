@@ -121,6 +121,27 @@ def test_plan_validation_errors():
         assert _create(sv) == _lib.PSV_ERR_CUDA  # valid survey, no device: no CPU fallback
 
 
+def _tiny_survey(nz=40, nx=40, nshot=1, nt=4):
+    return S.Survey(nt=nt, nz=nz, nx=nx, dt=1e-4, dz=1.0, dx=1.0, npml=(0, 0, 0, 0),
+                    nshot=nshot, z_src=np.full(nshot, 5), x_src=np.full(nshot, 5),
+                    src_shot_to_fire=np.arange(nshot), stf_z=np.zeros((nshot, nt)),
+                    stf_x=np.zeros((nshot, nt))).finalize()
+
+
+def test_survey_size_limits():
+    """Blocks of grid rows and the shots of a batch map to CUDA grid
+    dimensions (at most 65535 each): larger surveys are refused before any
+    device work; the limits themselves are accepted."""
+    no_device = _lib.PSV_ERR_CUDA if not _lib.device_available() else _lib.PSV_OK
+    assert _create(_tiny_survey(nz=_lib.PSV_MAX_NZ + 1)) == _lib.PSV_ERR_UNSUPPORTED
+    assert b"nz above 65535" in _lib.lib().psv_last_error()
+    assert _create(_tiny_survey(nshot=_lib.PSV_MAX_SHOTS + 1)) == _lib.PSV_ERR_UNSUPPORTED
+    assert b"nshot above 65535" in _lib.lib().psv_last_error()
+    if no_device:
+        assert _create(_tiny_survey(nz=_lib.PSV_MAX_NZ)) == no_device
+        assert _create(_tiny_survey(nshot=_lib.PSV_MAX_SHOTS)) == no_device
+
+
 def _header_struct_fields(name):
     """Field names of `typedef struct name {...} name;` in declaration order."""
     text = open(helpers.__file__.replace("tests/helpers.py", "include/fwi_psv.h")).read()
