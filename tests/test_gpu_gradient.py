@@ -219,6 +219,36 @@ def test_survey_without_receivers(gpu, orc):
                 p.gradient()
 
 
+def test_silent_shot_follows_the_reference(gpu, orc):
+    # every source fires in shot 0, so shot 1 has no source: its traces and
+    # energies are zero, and the reference's scale_grad_E2
+    # (src/cpu/n_kernel_lib_PSV.cpp:760-783) divides its zero gradient by a
+    # zero energy weight, 0 / 0, over the whole energy window.  The engine
+    # does the same: NaN at the oracle's cells, its values elsewhere.
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=120, nz=41,
+                                  nx=61, nrec=6)
+    sv.src_shot_to_fire = np.zeros(sv.nsrc, np.int32)
+    sv.finalize()
+    uz, ux = orc.simulate_fwd(sv, *true)
+    assert not np.abs(uz[1]).any() and not np.abs(ux[1]).any()
+    with np.errstate(invalid="ignore", divide="ignore"):
+        L2_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz, ux)
+    nan_ref = [np.isnan(g) for g in g_ref]
+    assert all(m.any() for m in nan_ref)
+    for precision, tol in ((64, RTOL64), (32, RTOL32_GRAD)):
+        with engine.Plan(sv, precision=precision) as p:
+            p.set_model(*true)
+            fu, fx = p.forward()
+            assert not np.abs(fu[1]).any() and not np.abs(fx[1]).any()
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            L2, g = p.gradient()
+        assert L2 == pytest.approx(L2_ref, rel=tol)
+        for a, b, m in zip(g, g_ref, nan_ref):
+            assert np.array_equal(np.isnan(a), m)
+            assert helpers.rel_l2(a[~m], b[~m]) < tol
+
+
 def test_single_shot_with_chains_requested(gpu, orc):
     # one shot a batch: nothing to split, the plan runs one stream
     sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=1, nt=150)
