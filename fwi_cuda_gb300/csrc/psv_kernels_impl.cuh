@@ -162,6 +162,15 @@ __device__ __forceinline__ void cpml_velocity(const StepParams<T> &p, int shot, 
     }
 }
 
+// The snapshot history and the shot gradients are touched once per
+// imaging step, thousands of launches apart: streaming (evict-first) loads
+// and stores keep their lines from evicting the wavefields, which the next
+// launches read again from L2.
+template <typename T>
+__device__ __forceinline__ T ld_once(const T *a) { return __ldcs(a); }
+template <typename T>
+__device__ __forceinline__ void st_once(T *a, T v) { __stcs(a, v); }
+
 // gard_fwd_storage2 (forward: store the step's snapshot into `slot`) or
 // fwi_grad2 (adjoint: image against snapshot `slot`, CPU sign) at point
 // (iz, ix) of the snapshot window (src/cpu/n_kernel_lib_PSV.cpp:398-484).
@@ -177,20 +186,21 @@ __device__ __forceinline__ void snapshot_point(const StepParams<T> &p, int shot,
     const long long qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
     T *h = p.hist + (long long)shot * p.hist_shot_stride + (long long)slot * p.hist_slot_stride + qq;
     if (MODE != MODE_ADJ) {
-        h[H_SZZ * sp] = ozz;
-        h[H_SZX * sp] = ozx;
-        h[H_SXX * sp] = oxx;
-        h[H_VZ * sp] = vzn * p.inv_dt;
-        h[H_VX * sp] = vxn * p.inv_dt;
+        st_once(h + H_SZZ * sp, ozz);
+        st_once(h + H_SZX * sp, ozx);
+        st_once(h + H_SXX * sp, oxx);
+        st_once(h + H_VZ * sp, vzn * p.inv_dt);
+        st_once(h + H_VX * sp, vxn * p.inv_dt);
     } else {
-        const T fzz = h[H_SZZ * sp], fzx = h[H_SZX * sp], fxx = h[H_SXX * sp];
-        const T fvz = h[H_VZ * sp], fvx = h[H_VX * sp];
+        const T fzz = ld_once(h + H_SZZ * sp), fzx = ld_once(h + H_SZX * sp);
+        const T fxx = ld_once(h + H_SXX * sp);
+        const T fvz = ld_once(h + H_VZ * sp), fvx = ld_once(h + H_VX * sp);
         const T s1 = p.g1[i] * ((fzz + fxx) * (ozz + oxx));
         const T s23 = p.g2[i] * (fzx * ozx + T(0.25) * ((fzz - fxx) * (ozz - oxx)));
         T *g = p.gshot + (long long)shot * p.gshot_shot_stride + qq;
-        g[0] -= s1;
-        g[sp] -= s23 + s1;
-        g[2 * sp] -= p.kimg * (uxn * fvx + uzn * fvz);
+        st_once(g, ld_once(g) - s1);
+        st_once(g + sp, ld_once(g + sp) - (s23 + s1));
+        st_once(g + 2 * sp, ld_once(g + 2 * sp) - p.kimg * (uxn * fvx + uzn * fvz));
     }
 }
 
@@ -217,9 +227,10 @@ __device__ __forceinline__ ImagePre<T> image_preload(const StepParams<T> &p, int
     e.qq = (long long)(dzr / p.snap_dz) * p.snx_pitch + dxr / p.snap_dx;
     const T *h = p.hist + (long long)bz * p.hist_shot_stride + (long long)slot * p.hist_slot_stride + e.qq;
     const T *g = p.gshot + (long long)bz * p.gshot_shot_stride + e.qq;
-    e.h[0] = h[H_SZZ * sp]; e.h[1] = h[H_SZX * sp]; e.h[2] = h[H_SXX * sp];
-    e.h[3] = h[H_VZ * sp]; e.h[4] = h[H_VX * sp];
-    e.g[0] = g[0]; e.g[1] = g[sp]; e.g[2] = g[2 * sp];
+    e.h[0] = ld_once(h + H_SZZ * sp); e.h[1] = ld_once(h + H_SZX * sp);
+    e.h[2] = ld_once(h + H_SXX * sp);
+    e.h[3] = ld_once(h + H_VZ * sp); e.h[4] = ld_once(h + H_VX * sp);
+    e.g[0] = ld_once(g); e.g[1] = ld_once(g + sp); e.g[2] = ld_once(g + 2 * sp);
     e.g1 = p.g1[i];
     e.g2 = p.g2[i];
     return e;
@@ -234,9 +245,9 @@ __device__ __forceinline__ void image_apply(const StepParams<T> &p, int bz, cons
     const T s1 = e.g1 * ((fzz + fxx) * (ozz + oxx));
     const T s23 = e.g2 * (fzx * ozx + T(0.25) * ((fzz - fxx) * (ozz - oxx)));
     T *g = p.gshot + (long long)bz * p.gshot_shot_stride + e.qq;
-    g[0] = e.g[0] - s1;
-    g[sp] = e.g[1] - (s23 + s1);
-    g[2 * sp] = e.g[2] - p.kimg * (uxn * fvx + uzn * fvz);
+    st_once(g, e.g[0] - s1);
+    st_once(g + sp, e.g[1] - (s23 + s1));
+    st_once(g + 2 * sp, e.g[2] - p.kimg * (uxn * fvx + uzn * fvz));
 }
 
 // update_v2 (src/cpu/n_kernel_lib_PSV.cpp:243-270) of interior point i from
