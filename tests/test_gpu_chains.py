@@ -36,6 +36,24 @@ def test_chains_equal_one_stream(gpu, orc, nshot, max_batch, chains):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("storage,kw", [("full", {}), ("binomial", dict(checkpoint_slots=2))])
+def test_fp64_chains_equal_one_stream(gpu, orc, storage, kw):
+    # FP64 plans run the direct family, so they chain too; 6 shots in 4
+    # groups of 2, 2, 2 and none
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=6, nt=150, snap_dt=3)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    c1, L1, g1, f1 = _run(sv, init, uz, ux, precision=64, storage=storage, chains=1, **kw)
+    c2, L2, g2, f2 = _run(sv, init, uz, ux, precision=64, storage=storage, chains=4, **kw)
+    assert c1 == 1 and c2 == 4
+    assert L1 == L2
+    for a, b in zip(g1 + list(f1), g2 + list(f2)):
+        assert np.array_equal(a, b)
+    L_ref, g_ref, _ = helpers.oracle_gradient(orc, sv, init, uz, ux)
+    assert L2 == pytest.approx(L_ref, rel=1e-9)
+    for a, b in zip(g2, g_ref):
+        assert helpers.rel_l2(a, b) < 1e-9
+
+
 @pytest.mark.parametrize("storage,kw", [("checkpoint", dict(checkpoint_interval=37)),
                                         ("binomial", dict(checkpoint_slots=3))])
 def test_checkpointed_chains_equal_one_stream(gpu, orc, storage, kw):
