@@ -32,3 +32,29 @@ def test_reference_arm_prints_on_rank_zero_only():
     env = dict(os.environ, RANK="1", WORLD_SIZE="2")
     assert _run("--impl", "reference", "--steps", "1", "--warmup", "0", "--ref-nt", "4",
                 env=env) == []
+
+
+def _bench_module():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def test_roofline_byte_model_and_committed_traffic():
+    # the per-update byte model of the roofline and the ncu traffic it is
+    # compared with (profiles/dram_traffic.txt, read by the bench)
+    import pytest
+    b = _bench_module()
+    assert b.algorithmic_bytes("stress_fwd", 3) == b.algorithmic_bytes("stress_adj", 3) == 44.0
+    assert b.algorithmic_bytes("velocity_fwd", 3) == pytest.approx(44.0 + 20.0 / 3)
+    assert b.algorithmic_bytes("velocity_adj", 3) == pytest.approx(60.0 + 52.0 / 3)  # 77.3 B
+    assert b.algorithmic_bytes("velocity_adj", 1) == 112.0
+    tv, ts = b.read_traffic("k_velocity_adj"), b.read_traffic("k_stress_adj")
+    # below the algorithmic bytes of one 301 x 601 x 8 launch: the wavefields stay in L2
+    updates = 8 * 301 * 601  # 111.9 MB a velocity_adj launch at snap_dt = 3
+    assert b.algorithmic_bytes("velocity_adj", 3) * updates == pytest.approx(111.917e6, rel=1e-4)
+    assert 0 < tv < b.algorithmic_bytes("velocity_adj", 3) * updates
+    assert 0 < ts < b.algorithmic_bytes("stress_adj", 3) * updates
+    assert b.read_traffic("no_such_kernel") is None
