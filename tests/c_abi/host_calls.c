@@ -46,6 +46,20 @@ int main(void)
     CHECK(psv_gauss_filter_kernel(1, k) == PSV_ERR_ARG);
     CHECK(strlen(psv_last_error()) > 0);
     CHECK(strlen(psv_error_string(PSV_ERR_CUDA)) > 0);
+    {
+        /* a grid taller than a CUDA grid dimension is refused before any
+         * device work, with or without a GPU */
+        psv_grid g;
+        psv_shots s;
+        psv_plan *plan = NULL;
+        memset(&g, 0, sizeof g);
+        memset(&s, 0, sizeof s);
+        g.nt = 1;
+        g.nz = PSV_MAX_NZ + 1;
+        g.nx = 8;
+        CHECK(psv_plan_create(&g, &s, NULL, &plan) == PSV_ERR_UNSUPPORTED && plan == NULL);
+        CHECK(PSV_MAX_SHOT_ELEMS == 2147483647LL && PSV_MAX_SHOTS == 65535);
+    }
     printf("ok %d actions, device %d\n", n, psv_device_available());
     return 0;
 }

@@ -166,6 +166,16 @@ def test_ctypes_structs_match_the_header(cname, pyclass):
     assert [f[0] for f in pyclass._fields_] == _header_struct_fields(cname)
 
 
+def test_python_constants_match_the_header():
+    text = open(helpers.__file__.replace("tests/helpers.py", "include/fwi_psv.h")).read()
+    defs = dict(re.findall(r"#define (PSV_[A-Z0-9_]+) (\d+)(?:LL)?\b", text))
+    for name in ("PSV_MAX_NZ", "PSV_MAX_SHOTS", "PSV_MAX_SHOT_ELEMS"):
+        assert getattr(_lib, name) == int(defs[name]), name
+    for key, name in (("full", "PSV_STORE_FULL"), ("checkpoint", "PSV_STORE_CHECKPOINT"),
+                      ("binomial", "PSV_STORE_BINOMIAL")):
+        assert _lib.STORAGE[key] == int(defs[name])
+
+
 def test_options_reach_the_library_in_order():
     o = engine.options(precision=32, kernels="tma", autotune=False, rows_per_thread=8)
     raw = C.string_at(C.addressof(o), C.sizeof(o))
