@@ -162,10 +162,11 @@ __device__ __forceinline__ void cpml_velocity(const StepParams<T> &p, int shot, 
     }
 }
 
-// The snapshot history and the shot gradients are touched once per
-// imaging step, thousands of launches apart: streaming (evict-first) loads
+// The snapshot history (read by the adjoint thousands of launches after
+// the forward wrote it) and the shot gradients (revisited every snap_dt
+// steps) are touched once per imaging step: streaming (evict-first) loads
 // and stores keep their lines from evicting the wavefields, which the next
-// launches read again from L2.
+// launch reads again from L2.
 template <typename T>
 __device__ __forceinline__ T ld_once(const T *a) { return __ldcs(a); }
 template <typename T>
