@@ -43,3 +43,56 @@ def test_oracle_reproduces_reference_program_outputs(orc, golden):
         assert np.array_equal(o["rtf_uz"], golden[f"{NAME}/shot{s}_rtf_uz"])
         assert np.array_equal(o["rtf_ux"], golden[f"{NAME}/shot{s}_rtf_ux"])
         assert np.array_equal(o["history"]["vz"], golden[f"{NAME}/shot{s}_vz"])
+
+
+def _program_status(work):
+    from fwi_cuda_gb300 import _lib, engine
+    try:
+        engine.simulate_PSV(str(work))
+    except _lib.PSVError as e:
+        return e.status, str(e)
+    return _lib.PSV_OK, ""
+
+
+def test_program_input_errors(golden, tmp_path):
+    # simulate_PSV reads bin/*.bin (and io/*.bin for FWI) before any device
+    # work: a missing or short file is PSV_ERR_IO naming it, where the
+    # reference's readers (src/h_io_PSV.cpp) read on regardless
+    from fwi_cuda_gb300 import _lib
+    sv = helpers.load_case(golden, NAME)
+    model = golden[f"{NAME}/model"]
+    b = tmp_path / "bin"
+
+    def fresh(**kw):
+        for f in tmp_path.rglob("*.bin"):
+            f.unlink()
+        fio.write_inputs(str(tmp_path), sv, *model, **kw)
+
+    assert _program_status(tmp_path)[0] == _lib.PSV_ERR_IO  # nothing written yet
+    fresh()
+    (b / "metaint.bin").write_bytes((b / "metaint.bin").read_bytes()[:100])
+    st, msg = _program_status(tmp_path)
+    assert st == _lib.PSV_ERR_IO and "metaint.bin: short read" in msg
+    fresh()
+    meta = np.fromfile(b / "metaint.bin", np.int32)
+    meta[9] = 0  # nz
+    meta.tofile(b / "metaint.bin")
+    st, msg = _program_status(tmp_path)
+    assert st == _lib.PSV_ERR_IO and "invalid sizes" in msg
+    for name in ("intarray", "metafloat", "mat"):
+        fresh()
+        data = (b / f"{name}.bin").read_bytes()
+        (b / f"{name}.bin").write_bytes(data[:len(data) - 8])
+        st, msg = _program_status(tmp_path)
+        assert st == _lib.PSV_ERR_IO and f"{name}.bin" in msg, (name, msg)
+        (b / f"{name}.bin").unlink()
+        st, msg = _program_status(tmp_path)
+        assert st == _lib.PSV_ERR_IO and f"cannot open bin/{name}.bin" in msg, (name, msg)
+    fresh(fwinv=True, rtf_meas_true=False)
+    assert _program_status(tmp_path)[0] == _lib.PSV_ERR_ARG
+    fresh(fwinv=True)
+    st, msg = _program_status(tmp_path)
+    assert st == _lib.PSV_ERR_IO and "shot0_rtf_uz.bin" in msg
+    if not _lib.device_available():
+        fresh()  # complete inputs: the first device call fails, no CPU fallback
+        assert _program_status(tmp_path)[0] == _lib.PSV_ERR_CUDA
