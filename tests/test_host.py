@@ -195,3 +195,31 @@ def test_host_mat_av2_matches_oracle(orc):
     for x, y in zip(a[:3], b[:3]):
         assert np.array_equal(x, y)
     assert np.allclose(a[3], b[3], rtol=1e-12)
+
+
+def test_host_preprocessing_argument_errors():
+    # where the reference would index out of range or exit, the ABI returns
+    # a status and leaves a message
+    L = _lib.lib()
+    hc = np.zeros(7)
+    for fd, mre in ((3, 1), (14, 1), (0, 1), (4, 5), (4, -1)):
+        assert L.psv_holbergcoeff(fd, mre, dptr(hc)) == _lib.PSV_ERR_ARG, (fd, mre)
+    assert L.psv_holbergcoeff(12, 4, dptr(hc)) == _lib.PSV_OK
+    p = [np.zeros(40) for _ in range(6)]
+    args = (2.0, 3000.0, 0.001, 1.0, 100.0)
+    assert L.psv_cpml_PSV(*[dptr(a) for a in p], *args, 10, 10, 2, 40, 1e-4, 1.0) == _lib.PSV_OK
+    assert L.psv_cpml_PSV(*[dptr(a) for a in p], *args, 38, 0, 2, 40, 1e-4, 1.0) == _lib.PSV_ERR_ARG
+    assert b"do not fit" in L.psv_last_error()
+    assert L.psv_cpml_PSV(*[dptr(a) for a in p], *args, 0, 38, 2, 40, 1e-4, 1.0) == _lib.PSV_ERR_ARG
+    assert L.psv_cpml_PSV(*[dptr(a) for a in p], *args, 1, 1, 2, 0, 1e-4, 1.0) == _lib.PSV_ERR_ARG
+    s = np.zeros(10)
+    assert L.psv_wavelet(dptr(s), 10, 1e-4, 1.0, 100.0, 0.0, 2) == _lib.PSV_ERR_UNSUPPORTED
+    assert L.psv_wavelet(dptr(s), -1, 1e-4, 1.0, 100.0, 0.0, 1) == _lib.PSV_ERR_ARG
+    m = np.full((20, 20), 2000.0)
+    out = np.zeros(4)
+    L.psv_holbergcoeff(4, 1, dptr(hc))
+    assert L.psv_checkfd_ssg_elastic(20, 20, 1.0, 1e-5, 1e-2, 11, dptr(m), dptr(m * 1e6),
+                                     dptr(m * 1e6), dptr(hc), dptr(out)) == _lib.PSV_ERR_ARG
+    assert b"absorbing frame" in L.psv_last_error()
+    assert L.psv_checkfd_ssg_elastic(20, 20, 1.0, 1e-5, 1e-2, 5, dptr(m), dptr(m * 1e6),
+                                     dptr(m * 1e6), dptr(hc), dptr(out)) == _lib.PSV_OK
