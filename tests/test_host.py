@@ -82,6 +82,27 @@ def test_step_length_control_flow_matches_oracle(orc, fun, est, L0):
         assert rc == _lib.PSV_ERR_STEP_SEARCH
 
 
+def test_step_length_stops_at_a_failing_trial():
+    # a trial forward that fails (e.g. a device error) ends the search with
+    # its status; the estimate is left as it was and the trials done counted
+    calls = []
+
+    def trial(a, L, _):
+        calls.append(a)
+        if len(calls) == 3:
+            return _lib.PSV_ERR_CUDA
+        L[0] = (a - 0.037) ** 2
+        return 0
+
+    cb = _lib.TRIAL_FN(trial)
+    e, n = C.c_double(0.01), C.c_int(-1)
+    rc = _lib.lib().psv_step_length(C.byref(e), 0.037 ** 2, C.cast(cb, C.c_void_p), None,
+                                    C.byref(n), None, 0)
+    assert rc == _lib.PSV_ERR_CUDA and n.value == 2 and e.value == 0.01 and len(calls) == 3
+    assert _lib.lib().psv_step_length(C.byref(e), 1.0, None, None, None, None, 0) == \
+        _lib.PSV_ERR_ARG
+
+
 def test_calc_opt_step_matches_oracle(orc):
     rng = np.random.default_rng(0)
     for _ in range(50):
