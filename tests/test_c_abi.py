@@ -25,3 +25,20 @@ def test_plain_c_caller(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stdout + out.stderr
     assert out.stdout.startswith("ok ")
+
+
+def test_reference_side_binding_compiles_and_links(tmp_path):
+    # the C++ the reference's GPU branch would hold (the integration guide's
+    # example), against the header and the library's exported symbols
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    _lib.lib()
+    so = _lib.LIB
+    exe = tmp_path / "reference_binding"
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c_abi", "reference_binding.cpp"), "-o", str(exe),
+                    so, "-Wl,-rpath," + os.path.dirname(so)], check=True)
+    # GPU_CODE is 0 in the test binary: it links and exits without device work
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stdout + out.stderr
