@@ -244,3 +244,22 @@ def test_host_preprocessing_argument_errors():
     assert b"absorbing frame" in L.psv_last_error()
     assert L.psv_checkfd_ssg_elastic(20, 20, 1.0, 1e-5, 1e-2, 5, dptr(m), dptr(m * 1e6),
                                      dptr(m * 1e6), dptr(hc), dptr(out)) == _lib.PSV_OK
+
+
+def test_every_plan_call_refuses_a_null_plan():
+    # the status-returning plan calls give PSV_ERR_ARG for a null handle
+    # (never a crash), destroy accepts it, the queries give 0 / NULL
+    L = _lib.lib()
+    plan_calls = [n for n, (_, a) in _lib.SIGNATURES.items()
+                  if a and a[0] is C.c_void_p and n != "psv_misfit_noalloc"]
+    assert len(plan_calls) >= 20
+    for n in plan_calls:
+        res, argt = _lib.SIGNATURES[n]
+        args = [None] + [0 if t in (C.c_int, C.c_double) else None for t in argt[1:]]
+        got = getattr(L, n)(*args)
+        if n == "psv_plan_destroy":
+            assert got == _lib.PSV_OK
+        elif res is C.c_int:
+            assert got == _lib.PSV_ERR_ARG, n
+        else:
+            assert not got, n
