@@ -263,3 +263,18 @@ def test_every_plan_call_refuses_a_null_plan():
             assert got == _lib.PSV_ERR_ARG, n
         else:
             assert not got, n
+
+
+def test_compute_calls_refuse_null_arguments():
+    # checked before any device work: the CPU container gives the same
+    # statuses as a GPU machine
+    L = _lib.lib()
+    assert L.psv_multi_forward(None, 0, None, None) == _lib.PSV_ERR_ARG
+    assert L.psv_multi_gradient(None, 0, None) == _lib.PSV_ERR_ARG
+    assert L.psv_multi_forward((C.c_void_p * 2)(None, None), 2, None, None) == _lib.PSV_ERR_ARG
+    assert L.psv_misfit(None, None, None, None, None, None, 1, 1, 1, 1.0, None) == _lib.PSV_ERR_ARG
+    assert L.psv_misfit_noalloc(None, None, None, None, None, None, 1, 1, 1, 1.0, None,
+                                None) == _lib.PSV_ERR_ARG
+    assert L.psv_simulate_PSV(None, 0, -1, None) == _lib.PSV_ERR_ARG
+    assert L.psv_apply_gauss_filter(None, 5, 5, 2) == _lib.PSV_ERR_ARG
+    assert L.psv_PCG_PSV(None, None, None, 5, 5) == _lib.PSV_ERR_ARG
