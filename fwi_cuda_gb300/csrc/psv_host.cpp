@@ -214,6 +214,13 @@ extern "C" int psv_step_length(double *est_io, double L2_0, psv_trial_fn trial, 
                                int *ntrials, double *tlog, int max_trials)
 {
     if (!est_io || !trial) return psv::fail(PSV_ERR_ARG, "step_length: null estimate or trial");
+    // A misfit that is not a number (a NaN gradient: a shot whose sources
+    // never fire, nt = 1) makes every comparison below false, and the
+    // reference's search never ends; here it fails instead.
+    if (std::isnan(L2_0)) {
+        if (ntrials) *ntrials = 0;
+        return psv::fail(PSV_ERR_STEP_SEARCH, "step length search: misfit is not a number");
+    }
     const double scalefac = 2.0, stepmax_1 = 30, stepmax_2 = 4;
     double L2_test[3] = {L2_0, 0.0, 0.0}, sl[3] = {0.0, 0.0, 0.0};
     unsigned step1 = 0, step2 = 0, itests = 1, iteste = 1, countstep = 0;
@@ -235,6 +242,11 @@ extern "C" int psv_step_length(double *est_io, double L2_0, psv_trial_fn trial, 
                 tlog[2 * n + 1] = L2t;
             }
             n++;
+            if (std::isnan(L2t)) {
+                if (ntrials) *ntrials = n;
+                return psv::fail(PSV_ERR_STEP_SEARCH,
+                                 "step length search: trial misfit is not a number");
+            }
         }
         if ((step1 == 0) && (L2_test[0] <= L2_test[1])) {  // no decrease yet: halve
             est = est / scalefac;

@@ -1009,6 +1009,9 @@ static int step_length(const orc_grid *g, const orc_shots *s, work_t *w, double 
     const size_t nr = (size_t)s->nrec * g->nt;
     double est_step_length = *est;
     *ntrial = 0;
+    /* NaN misfits (a NaN gradient) make every comparison false and the
+     * reference's loop endless; the engine fails there, so does this. */
+    if (isnan(L2_0)) return -1;
     while ((step2 != 1) || (step1 != 1)) {
         double L2_tmp = 0;
         for (unsigned int itest = itests; itest <= iteste; itest++) {
@@ -1032,6 +1035,7 @@ static int step_length(const orc_grid *g, const orc_shots *s, work_t *w, double 
                 tlog[2 * *ntrial + 1] = L2_tmp;
             }
             (*ntrial)++;
+            if (isnan(L2_tmp)) return -1;
         }
         if ((step1 == 0) && (L2_test[0] <= L2_test[1])) {
             est_step_length = est_step_length / scalefac;
@@ -1073,6 +1077,7 @@ int orc_step_length_cb(double *est_io, double L2_0, orc_trial_fn fn, void *ctx, 
     unsigned int step1 = 0, step2 = 0, itests = 1, iteste = 1, countstep = 0;
     double est_step_length = *est_io;
     *ntrial = 0;
+    if (isnan(L2_0)) return -1; /* as in step_length above */
     while ((step2 != 1) || (step1 != 1)) {
         for (unsigned int itest = itests; itest <= iteste; itest++) {
             const double L2_tmp = fn(est_step_length, ctx);
@@ -1084,6 +1089,7 @@ int orc_step_length_cb(double *est_io, double L2_0, orc_trial_fn fn, void *ctx, 
                 tlog[2 * *ntrial + 1] = L2_tmp;
             }
             (*ntrial)++;
+            if (isnan(L2_tmp)) return -1;
         }
         if ((step1 == 0) && (L2_test[0] <= L2_test[1])) {
             est_step_length = est_step_length / scalefac;

@@ -103,6 +103,20 @@ def test_step_length_stops_at_a_failing_trial():
         _lib.PSV_ERR_ARG
 
 
+def test_step_length_fails_on_a_misfit_that_is_not_a_number(orc):
+    # the reference's search would loop for ever (every comparison with NaN
+    # is false); the engine and the oracle stop with a failure
+    nan = float("nan")
+    for L0, fun, trials in ((0.037 ** 2, lambda a: nan, 1), (nan, lambda a: a, 0),
+                            (0.037 ** 2, lambda a: (a - 0.037) ** 2 if a < 0.012 else nan, 2)):
+        rc, step, n, log = _step_length(0.01, L0, fun)
+        assert rc == _lib.PSV_ERR_STEP_SEARCH and n == trials and step == 0.01
+        assert b"not a number" in _lib.lib().psv_last_error()
+        rc2, _, n2, log2 = orc.step_length(0.01, L0, fun)
+        assert rc2 != 0 and n2 == trials
+        assert np.array_equal(log, log2, equal_nan=True)
+
+
 def test_calc_opt_step_matches_oracle(orc):
     rng = np.random.default_rng(0)
     for _ in range(50):

@@ -109,3 +109,75 @@ def test_fwi_matches_reference_library_surface_layout(orc):
     assert r1["rc"] == 0 and r2["rc"] == 0
     for k in ("L2", "step", "lam", "mu", "rho", "grad_lam", "grad_mu", "grad_rho"):
         assert np.array_equal(r1[k], r2[k]), k
+
+
+def _layout(name):
+    """FWI layouts for the reference-library pins; imaging_sign = 1 (the
+    reference's CUDA sign), the sign whose update lowers the misfit, so the
+    reference's step search succeeds."""
+    if name == "order6":
+        return helpers.case(fdorder=6, stencil="reference", nt=180, nz=51, nx=71, npml=8,
+                            nrec=12, imaging_sign=1)
+    if name == "subsampled":
+        sv, true, init = helpers.case(fdorder=4, stencil="reference", nt=180, nz=51, nx=71,
+                                      npml=8, nrec=12, snap_dt=3, imaging_sign=1)
+        sv.snap_dz, sv.snap_dx = 2, 3
+        sv.snap_z1, sv.snap_z2, sv.snap_x1, sv.snap_x2 = 5, sv.nz - 9, 7, sv.nx - 10
+        return sv, true, init
+    if name == "velocity_sources":
+        return helpers.crosswell(fdorder=2, stencil="reference", nt=250, nz=61, nx=51, nshot=2,
+                                 nrec=10)
+    if name == "side_surfaces":
+        sv, true, init = helpers.case(fdorder=2, stencil="reference", nt=180, nz=51, nx=71,
+                                      nrec=12, imaging_sign=1)
+        sv.isurf = (0, 0, 4, sv.nx - 6)
+        sv.npml = (10, 10, 0, 0)
+        sv.x_src = np.full(sv.nsrc, 12, np.int32)
+        sv.z_src = np.full(sv.nsrc, 30, np.int32)
+        return sv.finalize(), true, init
+    raise KeyError(name)
+
+
+def _fwi_against_reference(name):
+    """Run in a child process (the reference's error paths call exit):
+    one FWI iteration of the oracle and of the reference library."""
+    from oracle import oracle as O2
+    O2.build()
+    orc = O2.oracle()
+    orc.set_threads(1)
+    ref = O2.reference()
+    ref.set_threads(1)
+    sv, true, init = _layout(name)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    r1 = orc.simulate_fwi(sv, *init, uz, ux, niter=1)
+    r2 = ref.simulate_fwi(sv, *init, uz, ux, niter=1)
+    same = {k: bool(np.array_equal(r1[k], r2[k])) for k in
+            ("L2", "step", "lam", "mu", "rho", "grad_lam", "grad_mu", "grad_rho")}
+    return int(r1["rc"]), int(r2["rc"]), same
+
+
+@ref_only
+@pytest.mark.parametrize("name", ["order6", "subsampled", "velocity_sources", "side_surfaces"])
+def test_more_layouts_match_reference_library(name):
+    # one FWI iteration (forward, residuals, adjoint, imaging with the
+    # snapshot interpolation, energy preconditioning, step-length trials,
+    # update) of the oracle and of the reference's own code, bit for bit
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(1, mp_context=mp.get_context("spawn")) as pool:
+        rc1, rc2, same = pool.submit(_fwi_against_reference, name).result(timeout=600)
+    assert rc1 == 0 and rc2 == 0
+    assert all(same.values()), same
+
+
+def test_fwi_with_a_silent_shot_stops(orc):
+    # the gradient is NaN (0 / 0 in scale_grad_E2), so is the first trial's
+    # misfit: the reference's step search would loop for ever, the oracle
+    # (like the engine) reports a failed search after one trial
+    sv, true, init = helpers.case(fdorder=4, stencil="reference", nshot=2, nt=120, nz=41,
+                                  nx=61, nrec=6, imaging_sign=1)
+    sv.src_shot_to_fire = np.zeros(sv.nsrc, np.int32)
+    sv.finalize()
+    uz, ux = orc.simulate_fwd(sv, *true)
+    r = orc.simulate_fwi(sv, *init, uz, ux, niter=1)
+    assert r["rc"] != 0
