@@ -281,7 +281,9 @@ typedef int (*psv_trial_fn)(double step, double *L2, void *ctx);
  * 1.5 until a trial misfit rises again (at most 4 growths), then take the
  * parabola vertex (psv_calc_opt_step).  *est is the starting estimate in and
  * the accepted step out.  Trials are logged as (step, L2) pairs in tlog.
- * Returns PSV_ERR_STEP_SEARCH after 31 halvings without a decrease. */
+ * Returns PSV_ERR_STEP_SEARCH after 31 halvings without a decrease, and
+ * when L2_0 or a trial's L2 is NaN (a NaN gradient; the reference's loop
+ * never ends there). */
 int psv_step_length(double *est, double L2_0, psv_trial_fn trial, void *ctx, int *ntrials,
                     double *tlog, int max_trials);
 
