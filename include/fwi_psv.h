@@ -237,7 +237,10 @@ int psv_get_shot_gradient(psv_plan *plan, int ishot, double *grad_lam_shot,
  * shot, and update_mat2 of lam, mu, rho.  *step is the step-length estimate
  * carried between iterations (in: estimate, out: accepted step).  Outputs:
  * the iteration's L2, the number of trial forward passes and their (alpha,
- * L2) pairs in trial_log[2*k] (room for max_trials entries; may be NULL). */
+ * L2) pairs in trial_log[2*k] (room for max_trials entries; may be NULL).
+ * On PSV_ERR_STEP_SEARCH (where the reference exits, or loops for ever on a
+ * NaN misfit) the plan's model is the last trial's; psv_plan_set_model
+ * replaces it. */
 int psv_fwi_iteration(psv_plan *plan, double *step, double *L2, int *ntrials,
                       double *trial_log, int max_trials);
 

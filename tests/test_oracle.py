@@ -192,14 +192,21 @@ def test_more_layouts_match_reference_library(name):
     assert all(same.values()), same
 
 
-def test_fwi_with_a_silent_shot_stops(orc):
-    # the gradient is NaN (0 / 0 in scale_grad_E2), so is the first trial's
-    # misfit: the reference's step search would loop for ever, the oracle
-    # (like the engine) reports a failed search after one trial
+@pytest.mark.parametrize("cause", ["silent_shot", "zero_gradient"])
+def test_fwi_with_a_nan_update_stops(orc, cause):
+    # silent_shot: the gradient is NaN (0 / 0 in scale_grad_E2); zero_gradient
+    # (a one-cell window images nothing): update_mat2 scales by
+    # max|mat| / max|grad| = inf and inf * 0 is NaN.  Either way the first
+    # trial's misfit is NaN: the reference's step search would loop for ever,
+    # the oracle (like the engine) reports a failed search
     sv, true, init = helpers.case(fdorder=4, stencil="reference", nshot=2, nt=120, nz=41,
                                   nx=61, nrec=6, imaging_sign=1)
-    sv.src_shot_to_fire = np.zeros(sv.nsrc, np.int32)
+    if cause == "silent_shot":
+        sv.src_shot_to_fire = np.zeros(sv.nsrc, np.int32)
+    else:
+        sv.snap_z1 = sv.snap_z2 = 20
+        sv.snap_x1 = sv.snap_x2 = 30
     sv.finalize()
     uz, ux = orc.simulate_fwd(sv, *true)
     r = orc.simulate_fwi(sv, *init, uz, ux, niter=1)
-    assert r["rc"] != 0
+    assert r["rc"] != 0 and np.isnan(r["lam"]).any()
