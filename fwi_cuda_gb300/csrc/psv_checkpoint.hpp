@@ -49,6 +49,11 @@ struct CkAction {
     int op, seg, slot;
 };
 
+// A schedule lists every segment advance as an action: schedules with more
+// advances than this (a few slots forced on a very long record; 12 bytes an
+// action, 0.8 GB here) are refused before they are built.
+constexpr long long CK_MAX_ADVANCES = 1LL << 26;
+
 // beta(s, t) = C(s + t, t), saturated at 2^62.
 inline long long ck_beta(int s, int t)
 {

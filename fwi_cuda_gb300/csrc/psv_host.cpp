@@ -307,6 +307,9 @@ extern "C" int psv_checkpoint_schedule(int nseg, int slots, int *actions, int ca
                                        long long *advances)
 {
     if (nseg < 1 || slots < 1) return psv::fail(PSV_ERR_ARG, "need nseg >= 1 and slots >= 1");
+    if (psv::ck_min_advances(nseg, std::min(slots, nseg)) > psv::CK_MAX_ADVANCES)
+        return psv::fail(PSV_ERR_ARG, "checkpoint schedule: more than 2^26 segment advances; "
+                                      "give more slots");
     const psv::CkSchedule c = psv::ck_schedule(nseg, std::min(slots, nseg));
     const int n = (int)(c.fwd.size() + c.bwd.size());
     if (nactions) *nactions = n;

@@ -262,6 +262,10 @@ public:
         }
         if (ckpt) {
             store_kind = nck < nseg ? PSV_STORE_BINOMIAL : PSV_STORE_CHECKPOINT;
+            if (ck_min_advances(nseg, nck) > CK_MAX_ADVANCES)
+                return fail(PSV_ERR_UNSUPPORTED, "binomial checkpoints: more than 2^26 segment "
+                                                 "advances; give more checkpoint_slots or a "
+                                                 "longer checkpoint_interval");
             sched = ck_schedule(nseg, nck);
             fwd_slot.assign((size_t)nseg, -1);
             for (const CkAction &x : sched.fwd) fwd_slot[(size_t)x.seg] = x.slot;

@@ -98,3 +98,30 @@ def test_schedule_rejects_bad_arguments():
         engine.checkpoint_schedule(0, 3)
     with pytest.raises(_lib.PSVError):
         engine.checkpoint_schedule(5, 0)
+
+
+def test_schedules_beyond_the_advance_cap_are_refused_before_they_are_built():
+    # one action per segment advance: a few slots forced on a very long
+    # record would list 10^8..10^10 actions; the closed form refuses them at
+    # once (2^26 advances at most)
+    import time
+    from fwi_cuda_gb300 import _lib
+
+    def F(n, s):  # Griewank's closed form
+        if n <= 1:
+            return 0
+        if s == 1:
+            return n * (n - 1) // 2
+        t = 0
+        while comb(s + t, t) < n:
+            t += 1
+        return t * n - comb(s + t, t - 1)
+
+    assert all(F(n, s) == min_advances(n, s) for n in range(1, 40) for s in range(1, 6))
+    for n, slots in ((100000, 1), (11586, 1), (10 ** 6, 3)):
+        assert F(n, slots) > 2 ** 26
+        t = time.time()
+        with pytest.raises(_lib.PSVError) as e:
+            engine.checkpoint_schedule(n, slots)
+        assert e.value.status == _lib.PSV_ERR_ARG and time.time() - t < 1.0
+    assert F(11585, 1) <= 2 ** 26 and F(3334, 1) == 3334 * 3333 // 2
