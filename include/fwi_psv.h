@@ -366,7 +366,9 @@ int psv_plan_storage(const psv_plan *plan, int *storage, int *segment_steps, int
  * saves (op 1), then the adjoint pass (2 restore, 3 advance, 4 save the
  * working state, 5 recompute + reverse a segment) -- and their count into
  * *nactions, and the advances into *advances.  PSV_ERR_ARG if cap is too
- * small (the counts are still written). */
+ * small (the counts are still written), and for a schedule of more than
+ * 2^26 advances (every advance is an action; plan creation refuses those
+ * with PSV_ERR_UNSUPPORTED). */
 int psv_checkpoint_schedule(int nseg, int slots, int *actions, int cap, int *nactions,
                             long long *advances);
 
