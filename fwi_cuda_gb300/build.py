@@ -1,4 +1,5 @@
-"""Build the engine library ``fwi_cuda_gb300/_build/libfwi_psv.so``.
+"""Build the engine library ``fwi_cuda_gb300/_build/libfwi_psv.so`` and the
+program ``fwi_cuda_gb300/_build/seis_fwi`` linked to it.
 
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``), host C++ with g++; the units
@@ -18,6 +19,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libfwi_psv.so")
+EXE = os.path.join(OUT, "seis_fwi")  # the reference program's name, on this library
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
@@ -90,6 +92,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"linking failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    cmd = ["g++"] + CXX_FLAGS + [os.path.join(CSRC, "psv_main.cpp"), "-o", EXE, "-L", OUT,
+                                 "-lfwi_psv", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:  # the program is a convenience: the library stands without it
+        print(f"warning: linking seis_fwi failed:\n{r.stdout}\n{r.stderr}", file=sys.stderr)
     return LIB
 
 

@@ -96,3 +96,21 @@ def test_program_input_errors(golden, tmp_path):
     if not _lib.device_available():
         fresh()  # complete inputs: the first device call fails, no CPU fallback
         assert _program_status(tmp_path)[0] == _lib.PSV_ERR_CUDA
+
+
+def test_seis_fwi_program(golden, tmp_path):
+    # the reference's program name on the engine: a missing input is an error
+    # exit naming the file; complete inputs reach the device (on a machine
+    # without one, the CUDA error, never a CPU fallback)
+    import subprocess
+    from fwi_cuda_gb300 import _lib
+    from fwi_cuda_gb300 import build as B
+    _lib.lib()
+    assert os.path.exists(B.EXE)
+    out = subprocess.run([B.EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert out.returncode == 1 and "bin/metaint.bin" in out.stderr
+    if not _lib.device_available():
+        sv = helpers.load_case(golden, NAME)
+        fio.write_inputs(str(tmp_path), sv, *golden[f"{NAME}/model"])
+        out = subprocess.run([B.EXE, str(tmp_path)], capture_output=True, text=True, timeout=60)
+        assert out.returncode == 1 and "CUDA error" in out.stderr
