@@ -117,3 +117,50 @@ def test_two_rank_fwi_matches_single_process_oracle(orc):
     np.testing.assert_allclose(rows[:, 0], r["L2"], rtol=1e-11)
     np.testing.assert_allclose(rows[:, 1], r["step"], rtol=1e-9)
     assert list(rows[:, 2].astype(int)) == list(r["trials"])
+
+
+def _silent_worker(rank, world, port, out):
+    # shot 1 (rank 1's) has no source: the summed gradient is NaN, so is
+    # every rank's first trial misfit after the all-reduce, and every rank
+    # leaves the step search at that same trial (none is left waiting in a
+    # collective)
+    import datetime
+    import torch.distributed as dist
+    from fwi_cuda_gb300 import _lib
+    from oracle import oracle as O
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world, timeout=datetime.timedelta(seconds=60))
+    orc = O.oracle()
+    orc.set_threads(1)
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=120, nz=41, nx=61,
+                                  npml=8, nrec=6, imaging_sign=1)
+    sv.src_shot_to_fire = np.zeros(sv.nsrc, np.int32)
+    sv.finalize()
+    uz, ux = orc.simulate_fwd(sv, *true)
+    shots = parallel.shard_shots(sv.nshot, world, rank)
+    loc = parallel.shard_survey(sv, shots)
+    drv = parallel.DistributedFWI(OraclePlan(orc, loc, init, uz[shots], ux[shots]), sv.nz, sv.nx,
+                                  parallel.torch_allreduce())
+    try:
+        drv.iteration(0.01)
+        status = 0
+    except _lib.PSVError as e:
+        status = e.status
+    got = parallel.torch_allreduce()(np.array([float(status), 1.0]))
+    if rank == 0:
+        np.save(out, np.array([status, got[0], got[1]]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_fwi_stops_together_on_a_nan_misfit():
+    import torch.multiprocessing as mp
+    from fwi_cuda_gb300 import _lib
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = os.path.join(tempfile.mkdtemp(), "status.npy")
+    mp.spawn(_silent_worker, args=(2, port, out), nprocs=2, join=True)
+    status, total, ranks = np.load(out)
+    assert status == _lib.PSV_ERR_STEP_SEARCH and ranks == 2
+    assert total == 2 * _lib.PSV_ERR_STEP_SEARCH  # the same failure on both ranks
