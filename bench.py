@@ -38,23 +38,12 @@ CFG = dict(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=8, fdorder=4, stencil
 L2_BYTES = 129 * 2 ** 20
 
 
-def workload(nt=None, nshot=None):
+def workload(nt=None, nshot=None, setup=None):
+    """The surface FWI case (fwi_cuda_gb300.survey.surface_fwi_case): the
+    free surface sits on the first interior row, where the reference's
+    stress-image surface is stable with the full 4th-order stencil."""
     from fwi_cuda_gb300 import survey as S
-    c = dict(CFG)
-    if nt is not None:
-        c["nt"] = nt
-    if nshot is not None:
-        c["nshot"] = nshot
-    # Free surface on the first interior row.  With rows mirrored above it
-    # (the surface lower down), the reference's stress-image surface and the
-    # full 4th-order Holberg stencil grow without bound over nt = 4000 (x80
-    # every 500 steps in the FP64 oracle); on the first row it is stable.
-    sv, true, init = S.config_layered(nz=c["nz"], nx=c["nx"], dx=c["dx"], nt=c["nt"], dt=c["dt"],
-                                      nshot=c["nshot"], fdorder=c["fdorder"],
-                                      stencil=c["stencil"], npml=c["npml"], nrec=c["nrec"],
-                                      snap_dt=c["snap_dt"], seed=1234, surf_offset=0)
-    sv.imaging_sign = 1
-    return sv, true, init
+    return S.surface_fwi_case(nt=nt or CFG["nt"], nshot=nshot or CFG["nshot"], setup=setup)
 
 
 def config_dict(n_gpus, extra=None):
@@ -74,18 +63,31 @@ def updates_per_step(nt, nshot):
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_baseline(nt_sample=1000, threads=None):
+def product_library_loaded():
+    """True when the engine's libfwi_psv.so is mapped into this process."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libfwi_psv" in line for line in f)
+    except OSError:
+        return False
+
+
+def cpu_baseline(nt_sample=1000, threads=None, stencil="reference"):
     """One shot, forward + adjoint gradient, cropped to nt_sample steps, on the
     host cores: the reference's own code when oracle/_ref is built here, else
-    the oracle port (same loop structure and OpenMP placement)."""
+    the oracle port (same loop structure and OpenMP placement).  The survey's
+    set-up arrays come from that library's own functions, so the engine's
+    library is never loaded.  stencil "reference": the reference as written
+    (2-point difference x hc[1]); "holberg": the full 4th-order stencil the
+    engine runs (oracle port only: the reference has no such stencil)."""
     from oracle import oracle as O
     O.build()
-    kind = "reference" if O.ref_available() else "port"
+    kind = "reference" if O.ref_available() and stencil == "reference" else "port"
     lib = O.reference() if kind == "reference" else O.oracle()
     cores = threads or os.cpu_count()
     lib.set_threads(cores)
-    sv, true, init = workload(nt=nt_sample, nshot=1)
-    sv.stencil = "reference"  # the reference's stencil as written (2-point x hc[1])
+    sv, true, init = workload(nt=nt_sample, nshot=1, setup=lib)
+    sv.stencil = stencil
     lam, mu, rho = init
     mz, rz, rx, _ = lib.mat_av2(lam, mu, rho)
     t0 = time.perf_counter()
@@ -95,9 +97,11 @@ def cpu_baseline(nt_sample=1000, threads=None):
                    stf=(fwd["rtf_uz"], fwd["rtf_ux"]), src=src, rec=False)
     dt = time.perf_counter() - t0
     upd = 2.0 * nt_sample * CFG["nz"] * CFG["nx"]
+    what = ("reference 2-point stencil at fdorder 4" if stencil == "reference"
+            else "4th-order Holberg stencil (the engine's work)")
     return dict(value=upd / dt, unit=UNIT, cores=cores, kind=kind,
                 sample=f"1 shot forward+adjoint gradient, 301x601, nt={nt_sample} "
-                       f"(of 4000), reference 2-point stencil at fdorder 4, FP64, {dt:.1f} s")
+                       f"(of 4000), {what}, FP64, {dt:.1f} s")
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -613,12 +617,19 @@ def run_full_config(args):
 # ----------------------------------------------------------------------------- reference arm
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: each
-    step is a bounded sample (one shot forward + adjoint, nt cropped)."""
+    step is a bounded sample (one shot forward + adjoint, nt cropped).  Beside
+    it: the same sample on one thread, and the oracle port running the
+    engine's own 4th-order stencil on all cores.  The engine's library is
+    never loaded in this process (checked)."""
     for _ in range(args.warmup):
         cpu_baseline(nt_sample=args.ref_nt)
     vals = [cpu_baseline(nt_sample=args.ref_nt) for _ in range(args.steps)]
     v = float(np.mean([x["value"] for x in vals]))
     b = vals[-1]
+    one = cpu_baseline(nt_sample=max(20, args.ref_nt // 4), threads=1)
+    hol = cpu_baseline(nt_sample=args.ref_nt, stencil="holberg")
+    if product_library_loaded():
+        raise RuntimeError("the engine's library was loaded by the reference arm")
     upd = 2.0 * args.ref_nt * CFG["nz"] * CFG["nx"]
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": upd / v * 1e3,
@@ -626,6 +637,8 @@ def run_reference(args):
             "data": "synthetic (seeded layered model)", "config": config_dict(1),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": b["cores"], "kind": b["kind"],
                              "sample": b["sample"]},
+            "cpu_one_thread": one, "cpu_same_stencil": hol,
+            "engine_library_loaded": False,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -69,9 +69,9 @@ def _compile(src: str, extra: list, verbose: bool) -> str:
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(EXE):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(EXE))
     for d in (CSRC, os.path.join(ROOT, "include")):
         for f in os.listdir(d):
             if os.path.getmtime(os.path.join(d, f)) > t:

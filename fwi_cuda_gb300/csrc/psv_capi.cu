@@ -334,13 +334,15 @@ int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
 {
     if (!mod_z || !mod_x || !true_z || !true_x || !L2 || nshot <= 0 || nrec < 0 || nt < 0)
         return fail(PSV_ERR_ARG, "misfit: null array or bad size");
+    // the shots map to gridDim.y of the reduction
+    if (nshot > PSV_MAX_SHOTS) return fail(PSV_ERR_UNSUPPORTED, "misfit: nshot above 65535");
     if (!psv_device_available()) return fail(PSV_ERR_CUDA, "no CUDA device available");
     const long long n = (long long)nrec * nt;
     const size_t bytes = (size_t)nshot * n * sizeof(double);
     size_t total = 0;
     DevMem d[6], part, out;
     for (auto &m : d) PSV_TRY(m.alloc(bytes + 8, total));
-    PSV_TRY(part.alloc((size_t)256 * nshot * sizeof(double), total));
+    PSV_TRY(part.alloc((size_t)psv::kRedBlocks * nshot * sizeof(double), total));
     PSV_TRY(out.alloc((size_t)nshot * sizeof(double), total));
     const double *src[4] = {mod_z, mod_x, true_z, true_x};
     for (int k = 0; k < 4; k++) PSV_CU(cudaMemcpy(d[k].p, src[k], bytes, cudaMemcpyHostToDevice));

@@ -59,9 +59,13 @@ cudaError_t launch_adjoint_scale(const double *res_z, const double *res_x, long 
 // Deterministic FP64 sums: partial sums by a fixed grid, then one block.
 cudaError_t launch_model_sums(const double *lam, const double *mu, const double *rho, int nz,
                               int nx, double *partial, double *out3, cudaStream_t st);
+// Blocks of the first stage of the deterministic reductions: launch_adjsrc
+// writes kRedBlocks partial sums per shot, launch_model_sums 3 * kRedBlocks.
+constexpr int kRedBlocks = 256;
+
 // Residual res = mod - true (skipped when res_z is null) and L2 of nshot
 // shots, traces [shot][nt][nrec]; L2 of each shot into out[shot].  partial
-// needs nshot * 256 doubles.
+// needs nshot * kRedBlocks doubles.
 cudaError_t launch_adjsrc(const double *mod_z, const double *mod_x, const double *true_z,
                           const double *true_x, double *res_z, double *res_x,
                           long long n_per_shot, int nshot, double dt, double *partial,

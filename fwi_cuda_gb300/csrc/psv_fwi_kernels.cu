@@ -7,7 +7,7 @@
 
 namespace psv {
 
-static constexpr int RED_BLOCKS = 256;
+static constexpr int RED_BLOCKS = kRedBlocks;
 static constexpr int RED_THREADS = 256;
 
 // ---------------------------------------------------------------------------

@@ -3,10 +3,9 @@
 //
 // Who needs it: code that calls this library from inside another runtime's
 // memory discipline -- a host application whose GPU memory is all owned by a
-// framework allocator or a pre-sized pool, a caller recording a CUDA graph
-// (allocation calls are not allowed while a stream is being captured), or a
-// real-time loop that must not hit cudaMalloc/cudaFree latency or
-// fragmentation.  Those callers own their input and output buffers already;
+// framework allocator or a pre-sized pool (its own cudaMalloc would bypass
+// that accounting, and fail once the pool holds the device), or a real-time
+// loop that must not hit cudaMalloc/cudaFree latency or fragmentation.  Those callers own their input and output buffers already;
 // what psv_misfit would allocate beyond them is only scratch: the per-block
 // partial sums of the deterministic two-stage L2 reduction.  Here that
 // scratch is a fixed file-scope device array instead.
@@ -21,7 +20,11 @@
 
 namespace {
 
-constexpr int kPartialPerShot = 256;  // partial sums per shot (the reduction's grid)
+// Partial sums per shot: the first-stage grid of launch_adjsrc, whose
+// partial-sum buffer this array stands in for.
+constexpr int kPartialPerShot = psv::kRedBlocks;
+static_assert(kPartialPerShot * PSV_MISFIT_NOALLOC_MAX_SHOTS * sizeof(double) == (2u << 20),
+              "the scratch array's stated size (2 MiB) follows from the reduction's grid");
 
 // Scratch of every psv_misfit_noalloc call on a device: 256 partial sums per
 // shot for up to PSV_MISFIT_NOALLOC_MAX_SHOTS shots (2 MiB).  Each GPU that

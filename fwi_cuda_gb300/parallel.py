@@ -48,7 +48,15 @@ def shard_survey(sv, shots):
 
 
 class DistributedFWI:
-    """FWI iterations of a survey whose shots are split over ranks."""
+    """FWI iterations of a survey whose shots are split over ranks.
+
+    Every rank enters every collective, also after a local failure: a rank
+    whose gradient or trial forward raises contributes zeros and a failure
+    mark to the same all-reduce, so all ranks learn of it from that sum and
+    leave the iteration together with an error, instead of the others
+    waiting in a collective the failing rank never joins."""
+
+    NSTATUS = 16  # psv_status values are below this
 
     def __init__(self, plan, nz: int, nx: int, allreduce):
         """allreduce(np.ndarray float64) -> element-wise sum over ranks."""
@@ -56,13 +64,34 @@ class DistributedFWI:
         self.allreduce = allreduce
         self.G = [np.zeros((nz, nx)) for _ in range(3)]  # global gradient, after the taper
 
+    def _reduce(self, payload, status: int):
+        """Sum payload over ranks together with a count of the ranks that
+        failed, per status.  Returns (sum, highest failing status or 0)."""
+        marks = np.zeros(self.NSTATUS)
+        if status:
+            marks[min(int(status), self.NSTATUS - 1)] = 1.0
+        buf = self.allreduce(np.concatenate([np.ravel(payload), marks]))
+        counts = buf[-self.NSTATUS:]
+        failed = [k for k in range(1, self.NSTATUS) if counts[k] > 0.5]
+        return buf[:-self.NSTATUS], (max(failed) if failed else 0)
+
     def iteration(self, step: float, max_trials: int = 64):
         from . import _lib
         p = self.plan
         p.save_model()
         p.reset_gradient()
-        L2_loc, c = p.gradient()
-        buf = self.allreduce(np.concatenate([np.ravel(x) for x in c] + [np.array([L2_loc])]))
+        try:
+            L2_loc, c = p.gradient()
+            status, err = 0, None
+        except _lib.PSVError as e:
+            status, err = e.status, e
+            L2_loc, c = np.nan, [np.zeros_like(g) for g in self.G]
+        buf, failed = self._reduce(np.concatenate([np.ravel(x) for x in c] + [np.array([L2_loc])]),
+                                   status)
+        if failed:
+            if err is not None:
+                raise err
+            raise _lib.PSVError(failed, "gradient failed on another rank")
         n = c[0].size
         L2 = float(buf[-1])
         self.G = [g + buf[k * n:(k + 1) * n].reshape(g.shape) for k, g in enumerate(self.G)]
@@ -72,10 +101,14 @@ class DistributedFWI:
 
         def trial(a, L, _ctx):
             try:
-                L[0] = float(self.allreduce(np.array([p.trial_misfit(a)]))[0])
-                return 0
+                v, st = float(p.trial_misfit(a)), 0
             except _lib.PSVError as e:
-                return e.status
+                v, st = np.nan, e.status
+            tot, failed = self._reduce(np.array([v]), st)
+            if failed:
+                return failed
+            L[0] = float(tot[0])
+            return 0
 
         cb = _lib.TRIAL_FN(trial)
         est = C.c_double(step)

@@ -5,7 +5,11 @@ A :class:`Survey` holds what the reference reads from its binary inputs
 grid, CPML parameters, snapshot window, taper, sources and receivers.
 :meth:`Survey.finalize` derives the Holberg coefficients and the CPML
 profiles with the engine's host functions (``psv_holbergcoeff``,
-``psv_cpml_PSV``), exactly as ``simulate_PSV`` does.
+``psv_cpml_PSV``), exactly as ``simulate_PSV`` does.  Every builder takes
+an optional ``setup`` object with the same three set-up functions
+(``holbergcoeff(fdorder, maxrelerror)``, ``cpml(...)``, ``wavelet(...)``) in
+their place, so a caller that must not load the engine's library (a CPU
+baseline timed beside it) builds the same survey from its own copies.
 
 The generators below build the layered-plus-anomaly models of the
 benchmark configurations from a seed (no dataset is involved): horizontal
@@ -23,8 +27,11 @@ from . import _lib
 from ._lib import PsvGrid, PsvShots, dptr, f64, i32, iptr
 
 
-def ricker(nt: int, dt: float, fc: float, amp: float = 1.0, ts: float = 0.0) -> np.ndarray:
+def ricker(nt: int, dt: float, fc: float, amp: float = 1.0, ts: float = 0.0,
+           setup=None) -> np.ndarray:
     """Ricker wavelet of the reference (wavelet, src/h_preproc_PSV.cpp:267-286)."""
+    if setup is not None:
+        return np.asarray(setup.wavelet(nt, dt, amp, fc, ts, 1), np.float64)
     s = np.zeros(nt)
     _lib.check(_lib.lib().psv_wavelet(dptr(s), nt, dt, amp, fc, ts, 1))
     return s
@@ -82,17 +89,20 @@ class Survey:
     z_rec: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     x_rec: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
 
-    def finalize(self) -> "Survey":
-        """Holberg coefficients and CPML profiles (h_simulate_PSV.cpp:155-170)."""
+    def finalize(self, setup=None) -> "Survey":
+        """Holberg coefficients and CPML profiles (h_simulate_PSV.cpp:155-170),
+        from the engine's host functions or from ``setup``'s."""
         if self.fpad is None:
             self.fpad = self.fdorder // 2
-        self.hc = holbergcoeff(self.fdorder, 1)
+        hc_fn = setup.holbergcoeff if setup is not None else holbergcoeff
+        cpml_fn = setup.cpml if setup is not None else cpml_profiles
+        self.hc = np.asarray(hc_fn(self.fdorder, 1), np.float64)
         self.pml_z = bool(self.npml[0] or self.npml[1])
         self.pml_x = bool(self.npml[2] or self.npml[3])
-        z = cpml_profiles(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
-                          self.npml[0], self.npml[1], self.fpad, self.nz, self.dt, self.dz)
-        x = cpml_profiles(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
-                          self.npml[2], self.npml[3], self.fpad, self.nx, self.dt, self.dx)
+        z = cpml_fn(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
+                    self.npml[0], self.npml[1], self.fpad, self.nz, self.dt, self.dz)
+        x = cpml_fn(self.npower, self.damp_v_pml, self.rcoef, self.k_max_pml, self.freq_pml,
+                    self.npml[2], self.npml[3], self.fpad, self.nx, self.dt, self.dx)
         (self.a_z, self.b_z, self.K_z, self.a_half_z, self.b_half_z, self.K_half_z) = z
         (self.a_x, self.b_x, self.K_x, self.a_half_x, self.b_half_x, self.K_half_x) = x
         self.z_src, self.x_src = i32(self.z_src), i32(self.x_src)
@@ -316,7 +326,7 @@ def load_profile_csv(path):
 
 def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml=20, nshot=1,
                    nrec=120, rec_spacing=4, src_depth=4, rec_depth=2, fc=100.0, vp_max=3000.0,
-                   snap_dt=1, surf_offset=None, force="z", seed=0) -> Survey:
+                   snap_dt=1, surf_offset=None, force="z", seed=0, setup=None) -> Survey:
     """Free surface on top, CPML on the other three sides, shots evenly
     spread along the surface, receivers on a line below the surface."""
     fpad = fdorder // 2
@@ -329,7 +339,7 @@ def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml
     else:
         x_src = np.linspace(x_rec[0] if nrec else npml + fpad + 4,
                             x_rec[-1] if nrec else nx - npml - fpad - 5, nshot).round()
-    w = ricker(nt, dt, fc)
+    w = ricker(nt, dt, fc, setup=setup)
     stf = np.stack([w] * nshot)
     zero = np.zeros_like(stf)
     snap_z1, snap_z2 = fpad, nz - fpad - 1
@@ -346,13 +356,13 @@ def surface_survey(nz, nx, dz, dx, nt, dt, *, fdorder=4, stencil="holberg", npml
                 src_shot_to_fire=np.arange(nshot), stf_z=stf if force == "z" else zero,
                 stf_x=zero if force == "z" else stf,
                 z_rec=np.full(nrec, isurf + rec_depth), x_rec=x_rec)
-    return sv.finalize()
+    return sv.finalize(setup)
 
 
 def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
                    stencil="holberg", npml=20, nrec=120, seed=1234, snap_dt=1, n_layers=5,
                    vp_range=(1800.0, 3000.0), anomaly_radius=15, smooth_sigma=15.0, fc=100.0,
-                   surf_offset=None):
+                   surf_offset=None, setup=None):
     """The 301 x 601 layered-plus-anomaly survey (one shot: forward + one
     adjoint gradient; eight shots: the FWI iteration case).  Smaller sizes
     give the same structure for tests.  surf_offset: free-surface row below
@@ -370,7 +380,30 @@ def config_layered(nz=301, nx=601, dx=0.5, nt=4000, dt=5e-5, nshot=1, fdorder=4,
     sv = surface_survey(nz, nx, dx, dx, nt, dt, fdorder=fdorder, stencil=stencil, npml=npml,
                         nshot=nshot, nrec=nrec, rec_spacing=rec_spacing, fc=fc,
                         vp_max=float(vp.max()), snap_dt=snap_dt, seed=seed,
-                        surf_offset=surf_offset)
+                        surf_offset=surf_offset, setup=setup)
+    return sv, true, init
+
+
+def surface_fwi_case(nt=4000, nshot=8, setup=None):
+    """The reference's surface FWI configuration at full size: 301 x 601
+    cells of 0.5 m, five horizontal layers (vp uniform in [1800, 3000] m/s,
+    increasing with depth) plus one +10 % Gaussian vp anomaly of 15-cell
+    radius (seed 1234), initial model = the true vp Gaussian-smoothed with
+    sigma = 15 cells; 4th-order Holberg stencil, free surface on the first
+    interior row and 20-cell CPML on the other sides; z-force 100 Hz Ricker
+    sources 2 m below the surface (one shot: x = 150 m; eight shots: evenly
+    along the receiver line), 120 receivers every 2 m at 1 m depth,
+    dt = 5e-5 s, nt = 4000, snapshots every 3 steps (the reference's example
+    setting, scripts/pre_proc_fwi.py:68), imaging sign +1 (the descent
+    direction).  The surface sits on the first interior row because with
+    rows mirrored above it the reference's stress-image free surface and
+    the full 4th-order Holberg stencil grow without bound over 4000 steps
+    (x80 every 500 steps in the FP64 oracle).
+    Returns (survey, true model, initial model)."""
+    sv, true, init = config_layered(nz=301, nx=601, dx=0.5, nt=nt, dt=5e-5, nshot=nshot,
+                                    fdorder=4, stencil="holberg", npml=20, nrec=120,
+                                    snap_dt=3, seed=1234, surf_offset=0, setup=setup)
+    sv.imaging_sign = 1
     return sv, true, init
 
 

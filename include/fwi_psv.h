@@ -255,9 +255,10 @@ int psv_misfit(const double *mod_z, const double *mod_x, const double *true_z,
 
 /* psv_misfit for callers that cannot allocate device memory.  No counterpart
  * in the reference.  Some callers may not call cudaMalloc: code whose GPU
- * memory is owned by a framework allocator or a fixed pool, a caller that is
- * recording a CUDA graph (allocation is not allowed during stream capture),
- * or a latency-bound loop that must avoid allocation.  They pass DEVICE
+ * memory is owned by a framework allocator or a fixed pool (an allocation of
+ * its own would bypass the owner's accounting and could fail once the pool
+ * holds the device's memory), or a latency-bound loop that must not pay for
+ * cudaMalloc/cudaFree or fragment the heap.  They pass DEVICE
  * pointers for every input and output (traces [nshot][nrec][nt], residuals
  * optional as a pair, d_L2[nshot]); the only scratch, the reduction's partial
  * sums, lives in a fixed device array inside the library (2 MiB, held by each

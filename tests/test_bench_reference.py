@@ -26,6 +26,24 @@ def test_reference_arm_json_line():
     assert r["e2e"] == {"value": r["value"], "unit": r["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
     assert r["config"]["nz"] == 301 and r["config"]["nx"] == 601
+    # a one-thread sample and the engine's own stencil on the port beside it;
+    # the engine's library stays out of the reference arm's process
+    assert r["cpu_one_thread"]["cores"] == 1 and r["cpu_one_thread"]["value"] > 0
+    assert r["cpu_same_stencil"]["kind"] == "port" and "Holberg" in r["cpu_same_stencil"]["sample"]
+    assert r["engine_library_loaded"] is False
+
+
+def test_reference_arm_builds_its_survey_without_the_engine():
+    # the oracle's set-up functions give the engine's survey bit for bit
+    from fwi_cuda_gb300 import survey as S
+    from oracle import oracle as O
+    a, ta, ia = S.surface_fwi_case(nt=40, nshot=2)
+    b, tb, ib = S.surface_fwi_case(nt=40, nshot=2, setup=O.oracle())
+    for k in ("hc", "a_z", "b_z", "K_z", "a_half_z", "b_half_z", "K_half_z", "a_x", "b_x", "K_x",
+              "a_half_x", "b_half_x", "K_half_x", "stf_z", "stf_x", "z_src", "x_src", "z_rec"):
+        assert (getattr(a, k) == getattr(b, k)).all(), k
+    for x, y in zip(ta + ia, tb + ib):
+        assert (x == y).all()
 
 
 def test_reference_arm_prints_on_rank_zero_only():

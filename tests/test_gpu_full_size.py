@@ -1,0 +1,84 @@
+"""Parity on the benchmark's own grid, at full length: the single-shot
+surface case (fwi_cuda_gb300.survey.surface_fwi_case with one shot:
+301 x 601, nt = 4000, 4th-order Holberg, free surface on the first interior
+row, 20-cell CPML, snapshots every 3 steps), forward and one adjoint
+gradient, engine against the FP64 oracle on the same inputs.
+
+Bars (the stated targets): FP32 seismogram relative L2 <= 1e-5, FP32
+gradient relative L2 <= 1e-4 for each of lam, mu, rho, FP32 misfit within
+1e-5; the FP64 engine within 1e-9 (only FMA contraction and reduction order
+differ from the oracle).  The measured FP32 errors are printed (run with -s)
+so they can be quoted.
+
+The oracle runs this case on all host cores (about a minute); its result is
+computed once per session and shared by the tests below."""
+import os
+
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import engine
+from fwi_cuda_gb300 import survey as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def single_shot(orc):
+    sv, true, init = S.surface_fwi_case(nshot=1)
+    orc.set_threads(os.cpu_count() or 1)
+    try:
+        uz, ux = orc.simulate_fwd(sv, *true)
+        L2, g, shots = helpers.oracle_gradient(orc, sv, init, uz, ux)
+    finally:
+        orc.set_threads(1)
+    return sv, true, init, uz, ux, L2, g, shots[0]
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_full_length_single_shot_forward_and_gradient(gpu, single_shot, precision):
+    sv, true, init, uz, ux, L2_ref, g_ref, shot_ref = single_shot
+    assert sv.nt == 4000 and (sv.nz, sv.nx) == (301, 601) and sv.nshot == 1
+    with engine.Plan(sv, precision=precision) as p:
+        p.set_model(*true)
+        fz, fx = p.forward()
+        p.set_model(*init)
+        p.set_observed(uz, ux)
+        L2, g = p.gradient()
+    e_seis = max(helpers.rel_l2(fz, uz), helpers.rel_l2(fx, ux))
+    e_grad = [helpers.rel_l2(a, b) for a, b in zip(g, g_ref)]
+    e_L2 = abs(L2 - L2_ref) / L2_ref
+    print(f"\nFP{precision} vs FP64 oracle, 301x601 nt=4000: seismogram {e_seis:.2e}, "
+          f"gradient lam/mu/rho {e_grad[0]:.2e}/{e_grad[1]:.2e}/{e_grad[2]:.2e}, "
+          f"misfit {e_L2:.2e} (L2 {L2_ref:.6e})")
+    # the residual is far above round-off (the FP32 gradient error grows as
+    # the trace error divided by the relative residual)
+    assert L2_ref > 0 and np.isfinite(L2)
+    if precision == 32:
+        assert e_seis <= 1e-5
+        assert max(e_grad) <= 1e-4
+        assert e_L2 <= 1e-5
+    else:
+        assert e_seis <= 1e-9
+        assert max(e_grad) <= 1e-9
+        assert e_L2 <= 1e-9
+
+
+def test_full_length_checkpointed_gradient_equals_full_storage(gpu, single_shot):
+    # binomial checkpointing recomputes the forward deterministically: the
+    # gradient equals the full-storage one bit for bit at full length too
+    sv, true, init, uz, ux, *_ = single_shot
+    out = {}
+    for storage in ("full", "checkpoint", "binomial"):
+        with engine.Plan(sv, precision=32, storage=storage, kernels="direct", rows_per_thread=1,
+                         block=(32, 4), chains=1, autotune=False) as p:
+            p.set_model(*init)
+            p.set_observed(uz, ux)
+            out[storage] = p.gradient()
+    L2f, gf = out["full"]
+    for storage in ("checkpoint", "binomial"):
+        L2c, gc = out[storage]
+        assert L2c == L2f, storage
+        for a, b in zip(gc, gf):
+            assert np.array_equal(a, b), storage

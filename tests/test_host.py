@@ -292,3 +292,14 @@ def test_compute_calls_refuse_null_arguments():
     assert L.psv_simulate_PSV(None, 0, -1, None) == _lib.PSV_ERR_ARG
     assert L.psv_apply_gauss_filter(None, 5, 5, 2) == _lib.PSV_ERR_ARG
     assert L.psv_PCG_PSV(None, None, None, 5, 5) == _lib.PSV_ERR_ARG
+
+
+def test_misfit_refuses_more_shots_than_a_launch_grid_holds():
+    # the shots of the misfit reduction map to gridDim.y: above 65535 the call
+    # fails with its own status before any device work, not a launch error
+    L = _lib.lib()
+    one = np.zeros(1)
+    rc = L.psv_misfit(dptr(one), dptr(one), dptr(one), dptr(one), None, None,
+                      _lib.PSV_MAX_SHOTS + 1, 1, 1, 1.0, dptr(one))
+    assert rc == _lib.PSV_ERR_UNSUPPORTED
+    assert b"65535" in L.psv_last_error()

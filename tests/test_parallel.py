@@ -164,3 +164,71 @@ def test_two_rank_fwi_stops_together_on_a_nan_misfit():
     status, total, ranks = np.load(out)
     assert status == _lib.PSV_ERR_STEP_SEARCH and ranks == 2
     assert total == 2 * _lib.PSV_ERR_STEP_SEARCH  # the same failure on both ranks
+
+
+class FailingPlan(OraclePlan):
+    """OraclePlan whose gradient or first trial forward fails on one rank."""
+
+    def __init__(self, *a, fail_in=None, status=None):
+        super().__init__(*a)
+        self.fail_in, self.status = fail_in, status
+
+    def gradient(self):
+        from fwi_cuda_gb300 import _lib
+        if self.fail_in == "gradient":
+            raise _lib.PSVError(self.status, "planted gradient failure")
+        return super().gradient()
+
+    def trial_misfit(self, step):
+        from fwi_cuda_gb300 import _lib
+        if self.fail_in == "trial":
+            raise _lib.PSVError(self.status, "planted trial failure")
+        return super().trial_misfit(step)
+
+
+def _one_rank_fails_worker(rank, world, port, out, where):
+    # only rank 1 fails (its gradient, or its first trial forward); rank 0
+    # must leave the iteration with the same status instead of waiting in
+    # the next all-reduce (the 60 s process-group timeout would end it with
+    # a different error)
+    import datetime
+    import torch.distributed as dist
+    from fwi_cuda_gb300 import _lib
+    from oracle import oracle as O
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank,
+                            world_size=world, timeout=datetime.timedelta(seconds=60))
+    orc = O.oracle()
+    orc.set_threads(1)
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nshot=2, nt=120, nz=41, nx=61,
+                                  npml=8, nrec=6, imaging_sign=1)
+    uz, ux = orc.simulate_fwd(sv, *true)
+    shots = parallel.shard_shots(sv.nshot, world, rank)
+    loc = parallel.shard_survey(sv, shots)
+    plan = FailingPlan(orc, loc, init, uz[shots], ux[shots],
+                       fail_in=where if rank == 1 else None, status=_lib.PSV_ERR_OOM)
+    drv = parallel.DistributedFWI(plan, sv.nz, sv.nx, parallel.torch_allreduce())
+    try:
+        drv.iteration(0.01)
+        status = 0
+    except _lib.PSVError as e:
+        status = e.status
+    got = parallel.torch_allreduce()(np.array([float(status), 1.0]))
+    if rank == 0:
+        np.save(out, np.array([status, got[0], got[1]]))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("where", ["gradient", "trial"])
+def test_two_rank_fwi_leaves_together_when_one_rank_fails(where):
+    import torch.multiprocessing as mp
+    from fwi_cuda_gb300 import _lib
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = os.path.join(tempfile.mkdtemp(), "status.npy")
+    mp.spawn(_one_rank_fails_worker, args=(2, port, out, where), nprocs=2, join=True)
+    status, total, ranks = np.load(out)
+    assert ranks == 2
+    assert status == _lib.PSV_ERR_OOM                 # rank 0 did not fail itself
+    assert total == 2 * _lib.PSV_ERR_OOM              # both ranks report the failure

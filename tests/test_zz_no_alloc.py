@@ -1,8 +1,8 @@
 """psv_misfit_noalloc: the misfit entry point that allocates nothing.
 
-Callers that cannot allocate device memory (framework-owned pools, CUDA-graph
-capture, allocation-free loops) hand it device buffers for the traces and
-results; the reduction's scratch is a fixed array inside the library.  This
+Callers that cannot allocate device memory (code whose GPU memory belongs to
+a framework allocator or a fixed pool, loops that must stay free of
+allocation latency) hand it device buffers for the traces and results; the reduction's scratch is a fixed array inside the library.  This
 test checks it through the C ABI against psv_misfit (the allocating entry
 point) on two calls in a row, so the second call runs on scratch the first
 one left behind.  The buffers here are allocated by the test with torch; the
