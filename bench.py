@@ -209,7 +209,7 @@ def plan_kernels(args):
     """Plan options for --kernels / --rpt (auto: the autotuner chooses)."""
     if args.kernels == "auto":
         return {}
-    dflt = {"tma": 4, "fused": 32}.get(args.kernels, 1)
+    dflt = {"tma": 4, "fused": 32, "march": 64}.get(args.kernels, 1)
     return dict(kernels=args.kernels, rows_per_thread=args.rpt or dflt, block=(32, args.by))
 
 
@@ -672,7 +672,7 @@ def main():
                     help="skip the 1001x2001 per-kernel bandwidth leg")
     ap.add_argument("--no-batching", action="store_true",
                     help="skip the plain-vs-batched shots/s comparison")
-    ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4", "fused"], default="auto",
+    ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4", "fused", "march"], default="auto",
                     help="time-step kernel family (auto: the plan's autotuner picks)")
     ap.add_argument("--rpt", type=int, default=0, help="rows per thread with --kernels")
     ap.add_argument("--by", type=int, default=4, help="thread-block height with --kernels")

@@ -35,6 +35,7 @@ UNITS = [
     ("psv_tiled.cu", []),
     ("psv_vec.cu", []),
     ("psv_fused.cu", []),
+    ("psv_march.cu", []),
     ("psv_fwi_kernels.cu", ["-fmad=false"]),
     ("psv_plan_f32.cu", []),
     ("psv_plan_f64.cu", []),

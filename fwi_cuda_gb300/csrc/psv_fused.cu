@@ -72,40 +72,6 @@ __device__ __forceinline__ void cp_async(float *dst, const float *src, bool in)
                      "r"(in ? 4 : 0) : "memory");
 }
 
-// cpml_stress with ping-ponged memories: reads copy `par`, and the owner of
-// the point writes copy 1 - par (halo points only read).
-__device__ __forceinline__ void cpml_stress_pp(const StepParams<float> &p, int shot, int iz, int ix,
-                                               float &vz_z, float &vx_z, float &vz_x, float &vx_x,
-                                               int par, bool own)
-{
-    static_assert(NMZ == NMX, "second copies at the same plane offset");
-    const int ro = par ? NMZ : 0, wo = par ? 0 : NMZ;
-    if (iz < p.pz0 || iz >= p.pz1) {
-        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-        float *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
-        const float m0 = p.b_z[iz] * m[(MZ_VZ + ro) * p.mz_plane] + p.a_z[iz] * vz_z;
-        const float m1 = p.bh_z[iz] * m[(MZ_VX + ro) * p.mz_plane] + p.ah_z[iz] * vx_z;
-        if (own) {
-            m[(MZ_VZ + wo) * p.mz_plane] = m0;
-            m[(MZ_VX + wo) * p.mz_plane] = m1;
-        }
-        vz_z = vz_z * p.ki_z[iz] + m0;
-        vx_z = vx_z * p.khi_z[iz] + m1;
-    }
-    if (ix < p.px0 || ix >= p.px1) {
-        const int c = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-        float *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + c;
-        const float m0 = p.b_x[ix] * m[(MX_VX + ro) * p.mx_plane] + p.a_x[ix] * vx_x;
-        const float m1 = p.bh_x[ix] * m[(MX_VZ + ro) * p.mx_plane] + p.ah_x[ix] * vz_x;
-        if (own) {
-            m[(MX_VX + wo) * p.mx_plane] = m0;
-            m[(MX_VZ + wo) * p.mx_plane] = m1;
-        }
-        vx_x = vx_x * p.ki_x[ix] + m0;
-        vz_x = vz_x * p.khi_x[ix] + m1;
-    }
-}
-
 // Shared-memory planes of one CTA.
 struct FusedSmem {
     float *vz, *vx, *zz, *zx, *xx;

@@ -50,6 +50,16 @@ bool fused_supported(int ns, int tz, int st, int sb, int sl, int sr, int nz1);
 cudaError_t launch_step_fused(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
                               int mode, int it, int slot, int par, int tz, int nbatch,
                               cudaStream_t st);
+// Fused time step as a vertical march (FP32, psv_march.cu): one launch per
+// step; a CTA of 32 warps threads owns 32 warps - 2 ns columns and `rows`
+// rows (32, 64 or 128) of one shot and walks down them, reading copy `par`
+// and writing copy 1 - par.  march_supported: no free surface or a top one
+// on the first interior row.
+bool march_supported(int ns, int rows, int warps, int st, int sb, int sl, int sr, int nz1);
+int march_tile_width(int ns, int warps);
+cudaError_t launch_step_march(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
+                              int mode, int it, int slot, int par, int rows, int warps, int nbatch,
+                              cudaStream_t st);
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
 cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,

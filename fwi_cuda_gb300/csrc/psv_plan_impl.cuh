@@ -158,10 +158,10 @@ public:
         const psv_grid &g = sv.g;
         const int nz = g.nz, nx = g.nx, nshot = sv.s.nshot, nrec = sv.s.nrec;
         const int al = 128 / (int)sizeof(T);
-        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_FUSED)
-            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2, 3 or 4");
+        if (opt.kernel_family < 0 || opt.kernel_family > PSV_KERNELS_MARCH)
+            return fail(PSV_ERR_ARG, "kernel_family must be 0, 1, 2, 3, 4 or 5");
         if (opt.kernel_family >= PSV_KERNELS_TMA && sizeof(T) != 4)
-            return fail(PSV_ERR_UNSUPPORTED, "TMA, VEC4 and FUSED kernels are FP32 only");
+            return fail(PSV_ERR_UNSUPPORTED, "TMA, VEC4, FUSED and MARCH kernels are FP32 only");
         if (opt.chains != 0 && opt.chains != 1 && opt.chains != 2 && opt.chains != 4)
             return fail(PSV_ERR_ARG, "chains must be 0 (autotuned), 1, 2 or 4");
         if (opt.smooth_hfs < 0 || opt.smooth_hfs == 1)
@@ -181,6 +181,13 @@ public:
             if (!fused_ok(rpt))
                 return fail(PSV_ERR_UNSUPPORTED, "fused time step: only a top free surface, within "
                                                  "the first tile row");
+        } else if (opt.kernel_family == PSV_KERNELS_MARCH) {
+            fam = PSV_KERNELS_MARCH;
+            rpt = march_rows(opt.rows_per_thread ? opt.rows_per_thread : 64);
+            blk = dim3(32, march_warps(opt.block_y > 0 ? opt.block_y : 4), 1);
+            if (!march_ok(rpt, (int)blk.y))
+                return fail(PSV_ERR_UNSUPPORTED, "march time step: no free surface or a top one on "
+                                                 "the first interior row only");
         } else {
             rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
             if (opt.block_y <= 0) blk = dim3(32, 4, 1);
@@ -337,7 +344,15 @@ public:
     // fused step; the working (recompute) state has 5 planes, 10 in FP32.
     static constexpr int nfield() { return sizeof(T) == 4 ? NFIELD_PP : NFIELD; }
     static constexpr int nwork() { return sizeof(T) == 4 ? 10 : 5; }
-    bool fused() const { return fam == PSV_KERNELS_FUSED; }
+    static int march_rows(int r) { return (r == 32 || r == 64 || r == 128) ? r : 64; }
+    static int march_warps(int w) { return (w == 2 || w == 4) ? w : 4; }
+    bool march_ok(int rows, int warps) const
+    {
+        return sizeof(T) == 4 &&
+               march_supported(sv.ns, rows, warps, sv.st, sv.sb, sv.sl, sv.sr, sv.nz1);
+    }
+    // One launch per step, v and sigma ping-ponged (FUSED tiles or MARCH strips).
+    bool fused() const { return fam == PSV_KERNELS_FUSED || fam == PSV_KERNELS_MARCH; }
     // Copy of v and sigma a step reads: step k of a pass reads copy k & 1
     // (the fused family ping-pongs; the others update in place, copy 0).
     int par(int k) const { return fused() ? (k & 1) : 0; }
@@ -393,7 +408,10 @@ public:
                      bool second, int pr)
     {
         if constexpr (sizeof(T) == 4)
-            if (fused()) return launch_step_fused(s, q, sv.ns, mode, it, slot, pr, rpt, B, st);
+            if (fam == PSV_KERNELS_MARCH)
+                return launch_step_march(s, q, sv.ns, mode, it, slot, pr, rpt, (int)blk.y, B, st);
+            else if (fused())
+                return launch_step_fused(s, q, sv.ns, mode, it, slot, pr, rpt, B, st);
         cudaError_t e = ks(s, second);
         if (e != cudaSuccess) return e;
         return kv(s, q, mode, it, slot, second);
@@ -554,12 +572,14 @@ public:
 
     // Sources and receivers bucketed by the velocity kernel's tiles (direct
     // family: 32 columns x blk.y * |rpt| rows; TMA: 64 x 4 rpt; VEC4: 128 x
-    // blk.y * rpt; FUSED: 64 x rpt), so each block finds its own.
+    // blk.y * rpt; FUSED: 64 x rpt; MARCH: 32 blk.y - fdorder x rpt), so each
+    // block finds its own.
     int build_tile_index()
     {
         const int nshot = sv.s.nshot, nrec = sv.s.nrec;
         const bool tma = fam == PSV_KERNELS_TMA, v4 = fam == PSV_KERNELS_VEC4;
-        const int tw = tma || fused() ? 64 : v4 ? 128 : 32;
+        const bool mr = fam == PSV_KERNELS_MARCH;
+        const int tw = mr ? march_tile_width(sv.ns, (int)blk.y) : tma || fused() ? 64 : v4 ? 128 : 32;
         const int tz = tma ? 4 * rpt : fused() ? rpt : (int)blk.y * (rpt < 0 ? -rpt : rpt);
         const int ntx = (sv.g.nx + tw - 1) / tw, ntz = (sv.g.nz + tz - 1) / tz;
         const int nt_ = ntx * ntz;
@@ -1350,12 +1370,16 @@ public:
     {
         if (f >= PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
         if (f == PSV_KERNELS_FUSED && !fused_ok(fused_tz(r))) f = PSV_KERNELS_DIRECT;
+        if (f == PSV_KERNELS_MARCH && !march_ok(march_rows(r), march_warps(by))) f = PSV_KERNELS_DIRECT;
         r = f == PSV_KERNELS_TMA     ? tma_rpt(r)
             : f == PSV_KERNELS_VEC4  ? v4_rpt(r)
             : f == PSV_KERNELS_FUSED ? fused_tz(r)
+            : f == PSV_KERNELS_MARCH ? march_rows(r)
                                      : rpt_ok<T>(r);
         if (f == PSV_KERNELS_TMA) by = 4;
         if (f == PSV_KERNELS_FUSED) by = (int)blk.y;  // unused
+        if (f == PSV_KERNELS_MARCH) by = march_warps(by);
+        if (f != PSV_KERNELS_MARCH && (by < 1 || by > 8)) by = 4;
         if (f == fam && r == rpt && (int)blk.y == by) return PSV_OK;
         fam = f;
         rpt = r;
@@ -1408,6 +1432,10 @@ public:
         if (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_FUSED)
             for (int tz : {16, 32})
                 if (fused_ok(tz)) cand.emplace_back(PSV_KERNELS_FUSED, tz, (int)blk.y);
+        if (opt.kernel_family == 0 || opt.kernel_family == PSV_KERNELS_MARCH)
+            for (int rows : {32, 64, 128})
+                for (int w : {2, 4})
+                    if (march_ok(rows, w)) cand.emplace_back(PSV_KERNELS_MARCH, rows, w);
         // 1) every candidate, launch by launch with CUDA events
         std::vector<std::pair<double, std::tuple<int, int, int>>> timed;
         for (auto &c : cand) {
@@ -1466,7 +1494,7 @@ public:
     {
         if (f) *f = fam;
         if (r) *r = rpt;
-        if (by) *by = fam == PSV_KERNELS_TMA ? 4 : fused() ? 0 : (int)blk.y;
+        if (by) *by = fam == PSV_KERNELS_TMA ? 4 : fam == PSV_KERNELS_FUSED ? 0 : (int)blk.y;
     }
 
     int prepare() override

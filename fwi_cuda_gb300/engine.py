@@ -20,7 +20,7 @@ from . import _lib
 from ._lib import PsvOptions, check, dptr, f64, i32, iptr
 
 
-FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused"}
+FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused", 5: "march"}
 
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
@@ -41,7 +41,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.chains = int(chains)
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
-    o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4}[kernels]
+    o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4, "march": 5}[kernels]
     return o
 
 

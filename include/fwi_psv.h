@@ -56,6 +56,9 @@ typedef enum {
 #define PSV_KERNELS_VEC4 3      /* four columns per thread, 128-bit loads and stores (FP32) */
 #define PSV_KERNELS_FUSED 4     /* one launch per time step: stress of a tile and its halo,
                                    then its velocities, from shared memory (FP32) */
+#define PSV_KERNELS_MARCH 5     /* one launch per time step: each CTA marches down a strip of
+                                   columns, stress then velocity row by row, stencil windows
+                                   in registers, rows staged ahead by cp.async (FP32) */
 
 /* Size limits (PSV_ERR_UNSUPPORTED above them).  The reference has none
  * besides memory; here grid rows and shots map to CUDA grid dimensions and
@@ -142,13 +145,16 @@ typedef struct psv_options {
                                    (balanced for CHECKPOINT, snap_dt for BINOMIAL) */
     int max_batch;              /* shots per launch; 0 = all shots of the survey */
     int use_graphs;             /* capture the time loop in CUDA graphs (default 1) */
-    int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32); 0 = default */
+    int block_x, block_y;       /* thread-block shape of the stencil kernels (block_x = 32;
+                                   MARCH family: block_y = warps per CTA, 2 or 4); 0 = default */
     int rows_per_thread;        /* rows each thread marches: direct family 1, 2, 4 (negative:
                                    warp-shuffle variant); TMA family 2, 4, 8; VEC4 family
-                                   1, 2, 4; FUSED family: tile rows 16 or 32; 0 = default */
+                                   1, 2, 4; FUSED family: tile rows 16 or 32; MARCH family:
+                                   rows each CTA marches, 32, 64 or 128; 0 = default */
     int kernel_family;          /* time-step kernels: 0 = any (the autotuner chooses),
-                                   PSV_KERNELS_DIRECT, _TMA, _VEC4 or _FUSED (the last three
-                                   FP32 only; FUSED needs no free surface but a top one) */
+                                   PSV_KERNELS_DIRECT, _TMA, _VEC4, _FUSED or _MARCH (the
+                                   last four FP32 only; FUSED needs no free surface but a top
+                                   one, MARCH none or a top one on the first interior row) */
     int autotune;               /* 1 (default): time the kernel candidates (family, tile
                                    shape and, for the direct family, the chain count) on the
                                    first gradient and keep the fastest (psv_plan_autotune);
@@ -348,8 +354,8 @@ int psv_last_timing(const psv_plan *plan, double *ms3);
 int psv_plan_autotune(psv_plan *plan, int nsteps, int *kernel_family, int *rows_per_thread,
                       int *block_y);
 /* The time-step kernels the plan launches now: family (PSV_KERNELS_*), rows
- * per thread (FUSED: tile rows) and block height (TMA: 4, FUSED: 0); any
- * pointer may be NULL. */
+ * per thread (FUSED: tile rows, MARCH: rows a CTA marches) and block height
+ * (TMA: 4, FUSED: 0, MARCH: warps per CTA); any pointer may be NULL. */
 int psv_plan_shape(const psv_plan *plan, int *kernel_family, int *rows_per_thread, int *block_y);
 /* Shot groups (streams) the plan's time loops run in: 1, 2 or 4. */
 int psv_plan_chains(const psv_plan *plan, int *chains);
