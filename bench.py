@@ -162,9 +162,9 @@ def algorithmic_bytes(prof_kernel, snap_dt):
             "velocity_adj": 36.0 + 16.0 + 8.0 + image}[prof_kernel]  # + u RW, We_adj RW
 
 
-def read_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic.txt")
+def read_traffic(kernel, name="dram_traffic.txt"):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -302,6 +302,7 @@ def run_ours(args, rank, world):
             r = p.fwi_iteration(0.01)
             fwi = dict(seconds=time.perf_counter() - t0, trials=r["ntrials"], step=r["step"])
     large = large_grid(args) if rank == 0 and not args.no_large else None
+    c3 = c3_cropped(args) if rank == 0 and not args.no_c3 else None
     uneven = uneven_batch(args) if rank == 0 and not args.no_uneven else None
     small = small_surveys(args) if rank == 0 and not args.no_uneven else None
     batching = None
@@ -311,13 +312,25 @@ def run_ours(args, rank, world):
 
     if rank != 0:
         return None
-    shares = dict(prof)
-    top = max(shares, key=shares.get)
-    pts = CFG["nz"] * CFG["nx"] * nshot
-    alg = algorithmic_bytes(top, CFG["snap_dt"]) * pts
-    achieved = alg / (prof[top] * 1e-3) / 1e9
     peak, src = peaks()
-    traffic = read_traffic(f"k_{top.split('_')[0]}_{top.split('_')[1]}")
+    pts = CFG["nz"] * CFG["nx"] * nshot
+    bench_kernels = {}
+    for k, v in prof.items():
+        if v <= 0:
+            continue
+        alg = algorithmic_bytes(k, CFG["snap_dt"]) * pts
+        bench_kernels[k] = {"ms": round(v, 5), "algorithmic_bytes": alg,
+                            "achieved_gbs": alg / (v * 1e-3) / 1e9,
+                            "frac": alg / (v * 1e-3) / 1e9 / peak}
+    if large:
+        roofline = large.pop("roofline")
+    else:  # no HBM-bound leg: the bench grid's dominant kernel, whose fields stay in L2
+        top = max(prof, key=prof.get)
+        alg = algorithmic_bytes(top, CFG["snap_dt"]) * pts
+        roofline = {"bound": "hbm", "kernel": top, "grid": "301x601x8 (L2-resident)",
+                    "achieved": alg / (prof[top] * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": alg / (prof[top] * 1e-3) / 1e9 / peak, "peak_source": src,
+                    "traffic": None, "algorithmic_bytes_per_launch": alg, "launch_ms": prof[top]}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -331,10 +344,10 @@ def run_ours(args, rank, world):
         "e2e": {"value": updates_per_step(nt, nshot) * world / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_s * 1e3},
-        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": src,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": alg,
-                     "launch_ms": prof[top], "kernel_ms": {k: round(v, 5) for k, v in prof.items()}},
+        "roofline": roofline,
+        # the bench grid's kernels: their 55 MB of wavefields stay in the L2, so
+        # these fractions of the HBM peak say little about HBM efficiency
+        "bench_grid_kernels": bench_kernels,
         "gpu_launches": launches,
         "clocks": clocks,
     }
@@ -345,24 +358,33 @@ def run_ours(args, rank, world):
         line["batching"] = batching
     if large:
         line["large_grid"] = large
+    if c3:
+        line["c3_cropped"] = c3
     if uneven:
         line["uneven_batch"] = uneven
     if small:
         line["small_surveys"] = small
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(nt_sample=args.cpu_nt)
+        line["cpu_one_thread"] = cpu_baseline(nt_sample=max(20, args.cpu_nt // 4), threads=1)
     return line
 
 
 def batching_compare(sv, init, obs_uz, obs_ux, shape, batched_shots_s):
-    """Shots/s of one FWI gradient along three paths on this GPU:
-    plain_dropin - the reference's per-shot structure through psv_kernel_PSV
-                   (kernel_PSV's interface): host model arrays, forward with
-                   the snapshot history returned to the host, host residual,
-                   adjoint fed the history back; shot 0 of the workload;
-    one_shot_plan - the plan with one shot per launch (device-resident);
-    checkpointed - the batched plan with checkpoint storage.
-    batched_vs_plain = the bench's batched shots/s / plain_dropin."""
+    """Shots/s of one FWI gradient of the bench survey along the plain and the
+    batched paths on this GPU:
+    plain        - the reference's GPU structure: one shot per launch
+                   (kernel_PSV_GPU, src/cuda/d_kernel_PSV.cu:16-220), the
+                   snapshot history resident on the device
+                   (src/cuda/d_alloc_PSV.cu:104): the plan with max_batch = 1
+                   and full storage;
+    checkpointed - every shot in one launch per half-step, checkpointed
+                   snapshot storage (two-level: one extra forward);
+    batched_full - every shot in one launch, full storage (the bench's value);
+    dropin_host_history - one shot through psv_kernel_PSV (kernel_PSV's
+                   interface) with the FP64 snapshot history returned to the
+                   host and fed back, host residual: the drop-in's price.
+    batched_vs_plain = checkpointed / plain."""
     from fwi_cuda_gb300 import engine, survey as S
     lam, mu, rho = init
     mz, rz, rx, _ = S.mat_av2(lam, mu, rho)
@@ -388,25 +410,29 @@ def batching_compare(sv, init, obs_uz, obs_ux, shape, batched_shots_s):
     res = (f["rtf_uz"] - obs_uz[0], f["rtf_ux"] - obs_ux[0])   # adjsrc2 residual
     call(True, res, (sv.z_rec, sv.x_rec, np.zeros(sv.nrec, np.int32), sv.rtf_type), 0,
          history=f["history"])
-    plain = 1.0 / (time.perf_counter() - t0)
+    dropin = 1.0 / (time.perf_counter() - t0)
     del f
 
     def plan_rate(**kw):
-        with engine.Plan(sv, precision=32, **shape, **kw) as p:
+        with engine.Plan(sv, precision=32, **dict(shape, **kw)) as p:
             p.set_model(*init)
             p.set_observed(obs_uz, obs_ux)
             p.gradient(fetch=False)  # warm-up (graph capture)
-            t0 = time.perf_counter()
-            p.gradient(fetch=False)  # returns after the stream is idle
-            return sv.nshot / (time.perf_counter() - t0)
+            t = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                p.gradient(fetch=False)  # returns after the stream is idle
+                t.append(time.perf_counter() - t0)
+            return sv.nshot / min(t), p.storage[0]
 
-    one = plan_rate(max_batch=1)
-    ck = plan_rate(storage="checkpoint")
-    return {"plain_dropin_shots_s": plain, "one_shot_plan_shots_s": one,
-            "checkpointed_shots_s": ck, "batched_shots_s": batched_shots_s,
-            "batched_vs_plain": batched_shots_s / plain,
-            "note": "plain_dropin: one shot through psv_kernel_PSV with the snapshot history "
-                    "on the host (host copies and layout conversion included)"}
+    plain, kind_p = plan_rate(max_batch=1, storage="full", chains=1)
+    ck, kind_c = plan_rate(storage="checkpoint")
+    return {"plain_shots_s": plain, "checkpointed_shots_s": ck,
+            "batched_full_shots_s": batched_shots_s, "batched_vs_plain": ck / plain,
+            "batched_full_vs_plain": batched_shots_s / plain,
+            "dropin_host_history_shots_s": dropin, "storage": [kind_p, kind_c],
+            "note": "plain: one shot per launch, history on the device (the reference's GPU "
+                    "structure); batched_vs_plain = checkpointed batch / plain"}
 
 
 LARGE = dict(nz=1001, nx=2001, dx=0.5, nt=300, dt=2.5e-5, nshot=8, fdorder=8, npml=30,
@@ -426,13 +452,32 @@ def large_workload(nt=None, nshot=None):
     return sv, true, init
 
 
+STEP_BYTES = {  # algorithmic bytes per grid-point update of a whole time step (FP32)
+    "forward": 60.0,   # v, sigma read + written once (40 B), 5 coefficients (20 B)
+    "adjoint": 84.0,   # + adjoint displacement u RW (16 B), We_adj RW (8 B)
+}
+
+
+def step_terms(snap_dt):
+    """Per-update bytes reported beside the step's: forward We RW (8 B) and
+    snapshot store (5 planes every snap_dt steps), adjoint imaging (history
+    read 20 B + 3 shot gradients RW 24 B every snap_dt steps)."""
+    return {"forward": 8.0 + 20.0 / snap_dt, "adjoint": 44.0 / snap_dt}
+
+
 def large_grid(args):
-    """Per-kernel bandwidth where the wavefields do not fit in L2: the
-    1001 x 2001, order-8 Holberg, 30-cell CPML grid of the batched-survey
-    configuration, 8 shots (577 MB of wavefields), time axis cropped to 300
-    steps.  Reports each kernel's algorithmic GB/s (the per-update bytes of
-    algorithmic_bytes x points / CUDA-event launch time) against the
-    measured HBM peak, and gradient throughput."""
+    """HBM-bound kernels: the 1001 x 2001, order-8 Holberg, 30-cell CPML grid
+    of the batched-survey configuration, 8 shots (577 MB of wavefields, far
+    above the 126 MB L2), time axis cropped to 300 steps.  Reports
+    - the headline roofline object: the dominant kernel's per-kernel
+      algorithmic bytes (algorithmic_bytes x points) / its CUDA-event launch
+      time, against the measured HBM copy bandwidth, with the ncu DRAM
+      traffic per launch (profiles/dram_traffic_large.txt, captured on two
+      shots and scaled to eight by the points processed);
+    - the forward and adjoint time steps' fractions on the whole-step bytes
+      (60 and 84 B per update), and with the We / snapshot-store and imaging
+      terms added;
+    - gradient throughput."""
     from fwi_cuda_gb300 import engine
     c = LARGE
     sv, true, init = large_workload()
@@ -452,16 +497,84 @@ def large_grid(args):
     peak, src = peaks()
     kern = {}
     for k, ms in prof.items():
+        if ms <= 0:  # one-launch families time the whole step as the velocity launch
+            continue
         alg = algorithmic_bytes(k, c["snap_dt"]) * pts
         kern[k] = {"ms": round(ms, 4), "algorithmic_bytes": alg,
                    "achieved_gbs": alg / (ms * 1e-3) / 1e9, "frac": alg / (ms * 1e-3) / 1e9 / peak}
+    step_ms = {"forward": prof["stress_fwd"] + prof["velocity_fwd"],
+               "adjoint": prof["stress_adj"] + prof["velocity_adj"]}
+    terms = step_terms(c["snap_dt"])
+    steps = {}
+    for d in ("forward", "adjoint"):
+        t = step_ms[d] * 1e-3
+        steps[d] = {"ms": round(step_ms[d], 4), "bytes_per_update": STEP_BYTES[d],
+                    "frac": STEP_BYTES[d] * pts / t / 1e9 / peak,
+                    "bytes_per_update_with_terms": STEP_BYTES[d] + terms[d],
+                    "frac_with_terms": (STEP_BYTES[d] + terms[d]) * pts / t / 1e9 / peak}
+    top = max(kern, key=lambda k: kern[k]["ms"])
+    fam_kernel = {"tma": "k_{}_tma", "direct": "k_{}", "vec4": "k_{}_v4", "fused": "k_step_fused",
+                  "march": "k_step_march"}[fam]
+    traffic = read_traffic(f"{fam_kernel.format(top.split('_')[0])}_{top.split('_')[1]}",
+                           "dram_traffic_large.txt")
+    roofline = {"bound": "hbm", "kernel": top, "family": fam,
+                "grid": "1001x2001x8 shots, order 8 (HBM-bound)",
+                "achieved": kern[top]["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                "frac": kern[top]["frac"], "peak_source": src, "traffic": traffic,
+                "algorithmic_bytes_per_launch": kern[top]["algorithmic_bytes"],
+                "launch_ms": kern[top]["ms"], "step": steps}
     return {"workload": "1001x2001, order-8 Holberg, 30-cell CPML, 8 shots, nt=300 (cropped), "
                         "FP32, snap_dt=3", "kernels": {"family": fam, "rows_per_thread": rpt,
                                                         "block_y": by},
             "updates_per_s": 2.0 * pts * c["nt"] / sec, "gradient_s": sec,
             "updates_per_s_forward": pts * c["nt"] / (tm["forward_ms"] * 1e-3),
             "updates_per_s_adjoint": pts * c["nt"] / (tm["adjoint_ms"] * 1e-3),
-            "peak_gbs": peak, "peak_source": src, "per_kernel": kern}
+            "peak_gbs": peak, "peak_source": src, "per_kernel": kern, "roofline": roofline}
+
+
+def c3_cropped(args, nt=240):
+    """The batched-survey configuration's 64 shots on its 1001 x 2001,
+    order-8 grid, time axis cropped to `nt` steps: one FWI gradient with the
+    full snapshot history and one with 64 checkpoints per shot (two-level),
+    both in two batches of 32 shots (the full history of 64 shots does not
+    fit the 180 GB budget at once, and the global gradient sums the batches
+    in order, so equal batches are what makes the comparison exact); the two
+    gradients must be equal bit for bit (recomputation is deterministic)."""
+    from fwi_cuda_gb300 import engine
+    c = dict(LARGE, nshot=64, nt=nt)
+    sv, true, init = large_workload(nt=nt, nshot=64)
+    out = {}
+    obs = None
+    for storage in ("full", "checkpoint"):
+        kw = dict(plan_kernels(args), storage=storage, max_batch=32)
+        if storage == "checkpoint":
+            kw["checkpoint_interval"] = -(-nt // 64)
+        with engine.Plan(sv, precision=32, **kw) as p:
+            if obs is None:
+                p.set_model(*true)
+                obs = p.forward()
+            p.set_model(*init)
+            p.set_observed(*obs)
+            p.gradient(fetch=False)  # tunes, captures the graphs
+            p.reset_gradient()
+            t0 = time.perf_counter()
+            L2, g = p.gradient()
+            sec = time.perf_counter() - t0
+            kind, seg, slots, _ = p.storage
+            out[storage] = dict(L2=L2, g=g, s=sec, kind=kind, seg=seg, slots=slots,
+                                gb=p.device_bytes / 1e9, shape=p.shape)
+    f, k = out["full"], out["checkpoint"]
+    equal = f["L2"] == k["L2"] and all(np.array_equal(a, b) for a, b in zip(f["g"], k["g"]))
+    diff = max(float(np.linalg.norm(b - a) / max(np.linalg.norm(a), 1e-300))
+               for a, b in zip(f["g"], k["g"]))
+    upd = 2.0 * c["nshot"] * nt * c["nz"] * c["nx"]
+    return {"workload": f"1001x2001, order 8, 64 shots, nt={nt} (cropped from 10000), FP32",
+            "full_s": f["s"], "checkpoint_s": k["s"],
+            "full_updates_per_s": upd / f["s"], "checkpoint_updates_per_s": upd / k["s"],
+            "checkpoint_segment_steps": k["seg"], "checkpoint_slots_per_shot": k["slots"],
+            "device_gb": {"full": f["gb"], "checkpoint": k["gb"]},
+            "kernels": dict(zip(("family", "rows_per_thread", "block_y"), f["shape"])),
+            "checkpointed_equals_full_bitwise": bool(equal), "max_rel_l2_difference": diff}
 
 
 UNEVEN = [  # (nz, nx, nt cropped, fdorder, npml, peak Hz): the uneven-batch grids, 4 shots each
@@ -670,6 +783,8 @@ def main():
                     help="skip the multi-survey legs (uneven grids, small surveys)")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the 1001x2001 per-kernel bandwidth leg")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="skip the 64-shot cropped batched-survey leg (full vs checkpointed)")
     ap.add_argument("--no-batching", action="store_true",
                     help="skip the plain-vs-batched shots/s comparison")
     ap.add_argument("--kernels", choices=["auto", "direct", "tma", "vec4", "fused", "march"], default="auto",

@@ -62,7 +62,7 @@ class PsvOptions(C.Structure):
         ("checkpoint_interval", C.c_int), ("max_batch", C.c_int), ("use_graphs", C.c_int),
         ("block_x", C.c_int), ("block_y", C.c_int), ("rows_per_thread", C.c_int),
         ("kernel_family", C.c_int), ("autotune", C.c_int), ("checkpoint_slots", C.c_int),
-        ("smooth_hfs", C.c_int), ("pcg", C.c_int), ("chains", C.c_int),
+        ("smooth_hfs", C.c_int), ("pcg", C.c_int), ("chains", C.c_int), ("adjoint", C.c_int),
     ]
 
 

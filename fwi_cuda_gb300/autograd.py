@@ -16,6 +16,10 @@ point by point; the mu term correlates at 0.998 with a scale near 1.2 (mu
 enters the stencil through harmonic averages at staggered points, the
 imaging condition is a point estimate); the reference's density term does
 not follow dL2/drho.
+
+A plan created with adjoint="exact" (FP64) returns instead the derivative
+of L2 itself, from the hand-transposed discrete adjoint of the time loop
+(PSV_ADJOINT_EXACT), on every cell of the grid.
 """
 from __future__ import annotations
 
@@ -44,13 +48,16 @@ class FWIMisfit(torch.autograd.Function):
         m = [t.detach().to("cpu", torch.float64).numpy() for t in (lam, mu, rho)]
         plan.set_model(*m)
         plan.reset_gradient()
-        L2, _ = plan.gradient(fetch=False)
+        L2, glob = plan.gradient(fetch=True)
         orient = -1.0 if sv.imaging_sign > 0 else 1.0  # -> +dL2/dm
-        g = [np.zeros((sv.nz, sv.nx)) for _ in range(3)]
-        for s in range(sv.nshot):
-            o = plan.shot_gradient(s)
-            for k, name in enumerate(("grad_lam", "grad_mu", "grad_rho")):
-                g[k] += orient * _full(sv, o[name])
+        if getattr(plan, "adjoint", "reference") == "exact":
+            g = [orient * x for x in glob]
+        else:
+            g = [np.zeros((sv.nz, sv.nx)) for _ in range(3)]
+            for s in range(sv.nshot):
+                o = plan.shot_gradient(s)
+                for k, name in enumerate(("grad_lam", "grad_mu", "grad_rho")):
+                    g[k] += orient * _full(sv, o[name])
         ctx.save_for_backward(*[torch.from_numpy(x).to(t.device, t.dtype)
                                 for x, t in zip(g, (lam, mu, rho))])
         return torch.tensor(L2, dtype=torch.float64, device=lam.device)

@@ -36,6 +36,7 @@ UNITS = [
     ("psv_vec.cu", []),
     ("psv_fused.cu", []),
     ("psv_march.cu", []),
+    ("psv_exact.cu", []),
     ("psv_fwi_kernels.cu", ["-fmad=false"]),
     ("psv_plan_f32.cu", []),
     ("psv_plan_f64.cu", []),

@@ -60,6 +60,33 @@ int march_tile_width(int ns, int warps);
 cudaError_t launch_step_march(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
                               int mode, int it, int slot, int par, int rows, int warps, int nbatch,
                               cudaStream_t st);
+// Exact discrete adjoint of the FP64 time loop (psv_exact.cu).  Work planes
+// of one shot slot: v-bar (2), two copies of sigma-bar (3 each), e-bar (4),
+// d-bar (4), and the derivatives of L2 with respect to dt (lam + 2 mu),
+// dt lam, dt mu_zx, dt / rho_z, dt / rho_x and, in row 0 of the last plane,
+// the top surface factor.
+enum {
+    EX_VBZ = 0, EX_VBX = 1, EX_SB0 = 2, EX_SB1 = 5, EX_EB = 8, EX_DB = 12,
+    EX_GC2 = 16, EX_GCL, EX_GCM, EX_GRZ, EX_GRX, EX_GFS, EXACT_WORK_PLANES
+};
+struct ExactBufs {
+    double *store;             // [nt][batch][8][plane]: d' (4), e' (4) of every step
+    long long step_stride;     // batch * 8 * plane
+    double *work;              // [batch][EXACT_WORK_PLANES][plane]
+    double *qz, *qx;           // adjoint CPML memories, layout of StepParams::memz / memx
+    const double *rsum_z, *rsum_x;  // receiver adjoint sources [shot][nt][nrec]
+};
+cudaError_t launch_exact_forward_step(const StepParams<double> &p, const SrcRecParams<double> &q,
+                                      const ExactBufs &X, int ns, int n, int nbatch, int maxsrc,
+                                      cudaStream_t st);
+cudaError_t launch_exact_revsum(double *res_z, double *res_x, int nt, int nrec, long long stride,
+                                double dt, double gain, int nbatch, cudaStream_t st);
+cudaError_t launch_exact_adjoint_step(const StepParams<double> &p, const SrcRecParams<double> &q,
+                                      const ExactBufs &X, int ns, int n, int sin, int sout,
+                                      int nbatch, int maxsrc, cudaStream_t st);
+cudaError_t launch_exact_chain(const StepParams<double> &p, const ExactBufs &X, const double *lam,
+                               const double *mu, const double *rho, double *gl, double *gm,
+                               double *gr, double dt, double sign, cudaStream_t st);
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
 cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,

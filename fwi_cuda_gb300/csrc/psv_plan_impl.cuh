@@ -82,6 +82,7 @@ public:
     // Optional preconditioners: smoothing scratch and filter; Fletcher-Reeves
     // state (dir, old for lam, mu, rho) and reduction partials.
     DevMem gtmp, gfilt, pcgbuf, pcgpart;
+    DevMem ex_store, ex_work, ex_q;  // exact adjoint: per-step derivatives, work planes, memories
     DevMem ck, fld2, memz2, memx2;
     StepParams<T> sp{}, sp2{};
     SrcRecParams<T> qf{}, qa{}, qk{}, qr{};
@@ -191,6 +192,15 @@ public:
         } else {
             rpt = rpt_ok<T>(opt.rows_per_thread ? opt.rows_per_thread : 1);
             if (opt.block_y <= 0) blk = dim3(32, 4, 1);
+        }
+        if (opt.adjoint != PSV_ADJOINT_REFERENCE && opt.adjoint != PSV_ADJOINT_EXACT)
+            return fail(PSV_ERR_ARG, "adjoint must be PSV_ADJOINT_REFERENCE or PSV_ADJOINT_EXACT");
+        if (opt.adjoint == PSV_ADJOINT_EXACT) {
+            if (sizeof(T) != 8) return fail(PSV_ERR_UNSUPPORTED, "exact adjoint: FP64 plans only");
+            if (sv.sb || sv.sl || sv.sr)
+                return fail(PSV_ERR_UNSUPPORTED, "exact adjoint: no free surface or a top one only");
+            if (sv.s.rtf_type != 0 || sv.s.nrec == 0)
+                return fail(PSV_ERR_UNSUPPORTED, "exact adjoint: displacement receivers (rtf_type 0) needed");
         }
         pitch = round_up(nx, al);
         plane = (long long)nz * pitch;
@@ -1100,6 +1110,7 @@ public:
     int gradient(double *L2) override
     {
         if (!have_model || !have_obs) return fail(PSV_ERR_ARG, "gradient: model and observed traces required");
+        if (opt.adjoint == PSV_ADJOINT_EXACT) return exact_gradient(L2);
         PSV_TRY(ensure_hist());
         PSV_TRY(maybe_autotune());
         PSV_TRY(coefficients(true, false));
@@ -1199,6 +1210,93 @@ public:
         return PSV_OK;
     }
 
+    // Exact discrete adjoint (psv_exact.cu): a forward pass storing the
+    // CPML-corrected derivatives of every step, residual and L2 (adjsrc2), the
+    // transposed steps in reverse time, then the chain rule into the global
+    // gradients as -imaging_sign * dL2/dm.  Batch by batch in shot order, one
+    // launch sequence per step (no graphs: verification-sized grids).
+    int exact_gradient(double *L2)
+    {
+        if constexpr (sizeof(T) != 8) {
+            (void)L2;
+            return fail(PSV_ERR_UNSUPPORTED, "exact adjoint: FP64 plans only");
+        } else {
+            const psv_grid &g = sv.g;
+            const int nt = g.nt, nshot = sv.s.nshot;
+            PSV_TRY(coefficients(true, false));
+            const size_t store_b = (size_t)nt * B * 8 * plane * sizeof(double);
+            const size_t work_b = (size_t)B * EXACT_WORK_PLANES * plane * sizeof(double);
+            const size_t q_b = (size_t)B * (mz_shot + mx_shot) * sizeof(double);
+            if (!ex_store.p) {
+                const double budget = (opt.hbm_budget_gb > 0 ? opt.hbm_budget_gb : 180.0) * 1e9;
+                if ((double)total + store_b + work_b + q_b > budget)
+                    return fail(PSV_ERR_OOM, "exact adjoint: the per-step derivatives (" +
+                                                 std::to_string(store_b >> 20) + " MiB) exceed the "
+                                                 "HBM budget; use fewer steps, shots per batch or "
+                                                 "a smaller grid");
+                PSV_TRY(ex_store.alloc(store_b, total));
+                PSV_TRY(ex_work.alloc(work_b, total));
+                PSV_TRY(ex_q.alloc(std::max<size_t>(q_b, 8), total));
+            }
+            ExactBufs X{};
+            X.store = ex_store.as<double>();
+            X.step_stride = (long long)B * 8 * plane;
+            X.work = ex_work.as<double>();
+            X.qz = ex_q.as<double>();
+            X.qx = ex_q.as<double>() + (size_t)B * mz_shot;
+            X.rsum_z = tr(4);
+            X.rsum_x = tr(5);
+            int maxsrc = 0;
+            for (int s_ = 0; s_ < nshot; s_++) maxsrc = std::max(maxsrc, h_f_off[s_ + 1] - h_f_off[s_]);
+            const double sign = sv.g.imaging_sign > 0 ? -1.0 : 1.0;
+            double tf = 0, ta = 0;
+            for (int b = 0; b < nbatch; b++) {
+                const int s0 = b * B, n = std::min(B, nshot - s0);
+                PSV_TRY(set_batch(b));
+                PSV_CU(cudaEventRecord(ev[0], st));
+                PSV_CU(launch_zero_planes<T>(fld.as<T>(), shot_stride, 0, shot_stride, B, st));
+                PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+                PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+                for (int it = 0; it < nt; it++) {
+                    PSV_CU(launch_exact_forward_step(sp, qf, X, sv.ns, it, B, maxsrc, st));
+                    nlaunch += 2 + (maxsrc ? 1 : 0) + 1;
+                }
+                PSV_CU(cudaEventRecord(ev[1], st));
+                PSV_CU(launch_adjsrc(tr(0) + s0 * ntr, tr(1) + s0 * ntr, tr(2) + s0 * ntr,
+                                     tr(3) + s0 * ntr, tr(4) + s0 * ntr, tr(5) + s0 * ntr, ntr, n,
+                                     g.dt, partial(), L2dev() + s0, st));
+                PSV_CU(launch_exact_revsum(tr(4) + s0 * ntr, tr(5) + s0 * ntr, nt, sv.s.nrec, ntr,
+                                           g.dt, g.dt / (g.dz * g.dx), n, st));
+                PSV_CU(cudaMemsetAsync(ex_work.p, 0, work_b, st));
+                PSV_CU(cudaMemsetAsync(ex_q.p, 0, ex_q.bytes, st));
+                int sin = EX_SB0, sout = EX_SB1;
+                for (int it = nt - 1; it >= 0; it--) {
+                    PSV_CU(launch_exact_adjoint_step(sp, qf, X, sv.ns, it, sin, sout, B, maxsrc, st));
+                    nlaunch += 4 + 1 + (maxsrc ? 1 : 0);
+                    std::swap(sin, sout);
+                }
+                PSV_CU(launch_exact_chain(sp, X, lam(), mu(), rho(), grad(0), grad(1), grad(2), g.dt,
+                                          sign, st));
+                PSV_CU(cudaEventRecord(ev[2], st));
+                PSV_TRY(sync_check());
+                float a, c;
+                PSV_CU(cudaEventElapsedTime(&a, ev[0], ev[1]));
+                PSV_CU(cudaEventElapsedTime(&c, ev[1], ev[2]));
+                tf += a;
+                ta += c;
+                last_s0 = s0;
+                last_n = n;
+            }
+            L2_shot.assign(nshot, 0.0);
+            PSV_CU(cudaMemcpy(L2_shot.data(), L2dev(), nshot * 8, cudaMemcpyDeviceToHost));
+            double s = 0.0;
+            for (int i = 0; i < nshot; i++) s += L2_shot[i];
+            if (L2) *L2 = s;
+            t_ms[0] = tf; t_ms[1] = ta; t_ms[2] = 0;
+            return PSV_OK;
+        }
+    }
+
     int get_gradient(double *gl, double *gm, double *gr) override
     {
         const size_t n = (size_t)sv.g.nz * sv.g.nx;
@@ -1229,6 +1327,9 @@ public:
     int get_shot(int ishot, double *gl, double *gm, double *gr, double *We, double *WeA,
                  double *uz, double *ux, double *L2) override
     {
+        if (opt.adjoint == PSV_ADJOINT_EXACT)
+            return fail(PSV_ERR_UNSUPPORTED, "get_shot_gradient: the exact adjoint has no per-shot "
+                                             "imaging terms");
         if (ishot < last_s0 || ishot >= last_s0 + last_n)
             return fail(PSV_ERR_ARG, "get_shot_gradient: shot not in the last gradient batch");
         const int b = ishot - last_s0;

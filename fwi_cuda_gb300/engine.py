@@ -25,7 +25,8 @@ FAMILIES = {1: "direct", 2: "tma", 3: "vec4", 4: "fused", 5: "march"}
 
 def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_graphs=True,
             block=(0, 0), checkpoint_interval=0, rows_per_thread=0, autotune=True,
-            kernels="any", checkpoint_slots=0, smooth_hfs=0, pcg=False, chains=0) -> PsvOptions:
+            kernels="any", checkpoint_slots=0, smooth_hfs=0, pcg=False, chains=0,
+            adjoint="reference") -> PsvOptions:
     o = PsvOptions()
     _lib.lib().psv_options_default(C.byref(o))
     o.precision = int(precision)
@@ -42,6 +43,7 @@ def options(precision=32, storage="auto", hbm_budget_gb=180.0, max_batch=0, use_
     o.rows_per_thread = int(rows_per_thread)
     o.autotune = int(bool(autotune))
     o.kernel_family = {"any": 0, "direct": 1, "tma": 2, "vec4": 3, "fused": 4, "march": 5}[kernels]
+    o.adjoint = {"reference": 0, "exact": 1}[adjoint]
     return o
 
 
@@ -91,6 +93,7 @@ class Plan:
         check(_lib.lib().psv_plan_create(C.byref(g), C.byref(s), C.byref(o), C.byref(h)))
         self.h = h
         self.n = survey.nz * survey.nx
+        self.adjoint = opts.get("adjoint", "reference")
 
     def close(self):
         if getattr(self, "h", None):

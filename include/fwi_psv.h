@@ -174,7 +174,23 @@ typedef struct psv_options {
                                    group's launches fill the others' kernel boundaries;
                                    checkpointed passes join them around every state copy);
                                    0 = the autotuner picks */
+    int adjoint;                /* PSV_ADJOINT_REFERENCE (default): the reference's imaging
+                                   condition (fwi_grad2) with its energy preconditioning;
+                                   PSV_ADJOINT_EXACT: the derivative of L2 itself (see below) */
 } psv_options;
+
+/* Adjoint modes (psv_options.adjoint).  EXACT has no counterpart in the
+ * reference: psv_gradient then accumulates -imaging_sign * dL2/dm (m = lam,
+ * mu, rho on every cell, no energy preconditioning) into the global
+ * gradients, computed by the hand-transposed discrete adjoint of the whole
+ * time loop (CPML, free surface, staggered averages, sources and receivers
+ * included), the same orientation the reference mode's imaging term has.
+ * FP64 plans only, no or a top free surface, displacement receivers
+ * (rtf_type 0); the forward stores 8 planes per step and shot, so it is for
+ * verification-sized grids (PSV_ERR_OOM beyond the budget).  Per-shot
+ * imaging terms (psv_plan_get_shot_gradient) do not exist in this mode. */
+#define PSV_ADJOINT_REFERENCE 0
+#define PSV_ADJOINT_EXACT 1
 
 void psv_options_default(psv_options *opt);
 

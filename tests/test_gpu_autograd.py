@@ -11,6 +11,8 @@ relative residual of that fit over the points, correlation):
   rho: reported only.  The reference's density imaging term does not follow
        dL2/drho: correlation -0.12 here (0.93 on a 61 x 91 model at nt 400).
        It is the reference's algorithm, kept for parity with its CPU path.
+The exact discrete adjoint (adjoint="exact") is held to tight bars on all
+three parameters: |c - 1| < 1e-2 and correlation > 0.999.
 """
 import numpy as np
 import pytest
@@ -75,3 +77,49 @@ def test_adjoint_gradient_against_finite_differences(gpu, imaging_sign):
     c, res, corr = fit["mu"]
     assert abs(c - 1) < 0.25 and corr > 0.99, fit["mu"]
     assert all(np.isfinite(v) for v in fit["rho"]), fit["rho"]
+
+
+def test_exact_adjoint_against_finite_differences(gpu):
+    # The same check with the exact discrete adjoint (adjoint="exact"): every
+    # parameter at tight bars (fitted scale within 1e-2 of 1, correlation
+    # above 0.999), the density included.
+    from fwi_cuda_gb300.autograd import misfit
+    sv, true, init = helpers.case(fdorder=4, stencil="holberg", nz=101, nx=201, nt=600, nshot=1,
+                                  snap_dt=1, imaging_sign=1)
+    with engine.Plan(sv, precision=64) as fwd:
+        fwd.set_model(*true)
+        obs = fwd.forward()
+
+        def value(m):
+            fwd.set_model(*m)
+            uz, ux = fwd.forward()
+            return 0.5 * sv.dt * (np.sum((uz - obs[0]) ** 2) + np.sum((ux - obs[1]) ** 2))
+
+        with engine.Plan(sv, precision=64, adjoint="exact") as p:
+            p.set_observed(*obs)
+            model = [torch.tensor(a, dtype=torch.float64, requires_grad=True) for a in init]
+            L2 = misfit(p, *model)
+            L2.backward()
+            grads = [m.grad.numpy() for m in model]
+        assert L2.item() == pytest.approx(value(init), rel=1e-12)
+        pts = _points(sv, 50)
+        base = [a.copy() for a in init]
+        fit = {}
+        for k, name in enumerate(("lam", "mu", "rho")):
+            fd, g = [], []
+            for iz, ix in pts:
+                h = 1e-3 * base[k][iz, ix]
+                mp = [a.copy() for a in base]
+                mm = [a.copy() for a in base]
+                mp[k][iz, ix] += h
+                mm[k][iz, ix] -= h
+                fd.append((value(mp) - value(mm)) / (2 * h))
+                g.append(grads[k][iz, ix])
+            fd, g = np.array(fd), np.array(g)
+            c = float(fd @ g / (g @ g))
+            fit[name] = (c, float(np.linalg.norm(fd - c * g) / np.linalg.norm(fd)),
+                         float(np.corrcoef(fd, g)[0, 1]))
+    print("exact adjoint, finite-difference fits (scale, residual, correlation):", fit)
+    for name in ("lam", "mu", "rho"):
+        c, res, corr = fit[name]
+        assert abs(c - 1) < 1e-2 and corr > 0.999, (name, fit[name])
