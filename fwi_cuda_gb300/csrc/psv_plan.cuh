@@ -34,6 +34,11 @@ struct TileMaps {
     CUtensorMap own;   // field planes, box 64 x 4 rpt
     CUtensorMap coef;  // coefficient planes, box 64 x 4 rpt
 };
+// 3-D tensor map (column, row, plane) over nplanes planes of nz x nx floats
+// (row pitch `pitch`, plane stride `plane` elements), box bx x by x 1, zero
+// fill outside (psv_tiled.cu).
+int encode3(CUtensorMap *map, const float *base, int nx, int nz, int pitch, long long plane,
+            int nplanes, int bx, int by);
 int encode_tile_maps(TileMaps *m, const float *fld, int nfplanes, const float *coef, int nx, int nz,
                      int pitch, long long plane, int ns, int rpt);
 // Four-columns-per-thread kernels (FP32, psv_vec.cu): blocks of 32 x by
@@ -51,15 +56,21 @@ cudaError_t launch_step_fused(const StepParams<float> &p, const SrcRecParams<flo
                               int mode, int it, int slot, int par, int tz, int nbatch,
                               cudaStream_t st);
 // Fused time step as a vertical march (FP32, psv_march.cu): one launch per
-// step; a CTA of 32 warps threads owns 32 warps - 2 ns columns and `rows`
-// rows (32, 64 or 128) of one shot and walks down them, reading copy `par`
-// and writing copy 1 - par.  march_supported: no free surface or a top one
-// on the first interior row.
-bool march_supported(int ns, int rows, int warps, int st, int sb, int sl, int sr, int nz1);
-int march_tile_width(int ns, int warps);
-cudaError_t launch_step_march(const StepParams<float> &p, const SrcRecParams<float> &q, int ns,
-                              int mode, int it, int slot, int par, int rows, int warps, int nbatch,
-                              cudaStream_t st);
+// step; a CTA of 256 threads owns 128 - 2 ns columns and `rows` rows (32, 64
+// or 128) of one shot and walks down them `stage` rows (2 or 4) at a time,
+// old v staged by TMA through the map of MarchMaps, reading copy `par` and
+// writing copy 1 - par.  march_supported: no free surface or a top one on the
+// first interior row.
+struct MarchMaps {
+    CUtensorMap fld;  // field planes, box (128 + 2 ns + 4) x stage
+};
+bool march_supported(int ns, int rows, int stage, int st, int sb, int sl, int sr, int nz1);
+int march_tile_width(int ns, int stage);
+int encode_march_maps(MarchMaps *m, const float *fld, int nfplanes, int nx, int nz, int pitch,
+                      long long plane, int ns, int stage);
+cudaError_t launch_step_march(const StepParams<float> &p, const SrcRecParams<float> &q,
+                              const MarchMaps &mm, int ns, int mode, int it, int slot, int par,
+                              int rows, int stage, int nbatch, cudaStream_t st);
 // Exact discrete adjoint of the FP64 time loop (psv_exact.cu).  Work planes
 // of one shot slot: v-bar (2), two copies of sigma-bar (3 each), e-bar (4),
 // d-bar (4), and the derivatives of L2 with respect to dt (lam + 2 mu),

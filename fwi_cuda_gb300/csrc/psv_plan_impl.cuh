@@ -67,6 +67,7 @@ public:
     int rpt = 1;                                     // rows per thread (< 0: shuffle variant)
     int fam = PSV_KERNELS_DIRECT;                    // kernel family of the time step
     TileMaps tmap{}, tmap2{};                        // tensor maps of fld / fld2 (TMA family)
+    MarchMaps mmap{}, mmap2{};                       // tensor maps of fld / fld2 (MARCH family)
     int *h_err = nullptr;                            // pinned copy of the device error word
     std::vector<int> h_f_off;                        // host copy of the per-shot source lists
     // Checkpointed storage: nck state slots at starts of K-step segments
@@ -185,7 +186,7 @@ public:
         } else if (opt.kernel_family == PSV_KERNELS_MARCH) {
             fam = PSV_KERNELS_MARCH;
             rpt = march_rows(opt.rows_per_thread ? opt.rows_per_thread : 64);
-            blk = dim3(32, march_warps(opt.block_y > 0 ? opt.block_y : 4), 1);
+            blk = dim3(32, march_stage(opt.block_y > 0 ? opt.block_y : 4), 1);
             if (!march_ok(rpt, (int)blk.y))
                 return fail(PSV_ERR_UNSUPPORTED, "march time step: no free surface or a top one on "
                                                  "the first interior row only");
@@ -355,7 +356,7 @@ public:
     static constexpr int nfield() { return sizeof(T) == 4 ? NFIELD_PP : NFIELD; }
     static constexpr int nwork() { return sizeof(T) == 4 ? 10 : 5; }
     static int march_rows(int r) { return (r == 32 || r == 64 || r == 128) ? r : 64; }
-    static int march_warps(int w) { return (w == 2 || w == 4) ? w : 4; }
+    static int march_stage(int w) { return (w == 2 || w == 4) ? w : 4; }
     bool march_ok(int rows, int warps) const
     {
         return sizeof(T) == 4 &&
@@ -373,8 +374,16 @@ public:
     int encode_maps()
     {
         if constexpr (sizeof(T) == 4) {
-            if (fam != PSV_KERNELS_TMA) return PSV_OK;
             const psv_grid &g = sv.g;
+            if (fam == PSV_KERNELS_MARCH) {
+                PSV_TRY(encode_march_maps(&mmap, fld.as<float>(), (int)(B * nfield()), g.nx, g.nz,
+                                          pitch, plane, sv.ns, (int)blk.y));
+                if (fld2.p)
+                    PSV_TRY(encode_march_maps(&mmap2, fld2.as<float>(), B * nwork(), g.nx, g.nz,
+                                              pitch, plane, sv.ns, (int)blk.y));
+                return PSV_OK;
+            }
+            if (fam != PSV_KERNELS_TMA) return PSV_OK;
             PSV_TRY(encode_tile_maps(&tmap, fld.as<float>(), (int)(B * nfield()), coef.as<float>(),
                                      g.nx, g.nz, pitch, plane, sv.ns, rpt));
             if (fld2.p)
@@ -419,7 +428,8 @@ public:
     {
         if constexpr (sizeof(T) == 4)
             if (fam == PSV_KERNELS_MARCH)
-                return launch_step_march(s, q, sv.ns, mode, it, slot, pr, rpt, (int)blk.y, B, st);
+                return launch_step_march(s, q, second ? mmap2 : mmap, sv.ns, mode, it, slot, pr, rpt,
+                                         (int)blk.y, B, st);
             else if (fused())
                 return launch_step_fused(s, q, sv.ns, mode, it, slot, pr, rpt, B, st);
         cudaError_t e = ks(s, second);
@@ -1471,7 +1481,7 @@ public:
     {
         if (f >= PSV_KERNELS_TMA && sizeof(T) != 4) f = PSV_KERNELS_DIRECT;
         if (f == PSV_KERNELS_FUSED && !fused_ok(fused_tz(r))) f = PSV_KERNELS_DIRECT;
-        if (f == PSV_KERNELS_MARCH && !march_ok(march_rows(r), march_warps(by))) f = PSV_KERNELS_DIRECT;
+        if (f == PSV_KERNELS_MARCH && !march_ok(march_rows(r), march_stage(by))) f = PSV_KERNELS_DIRECT;
         r = f == PSV_KERNELS_TMA     ? tma_rpt(r)
             : f == PSV_KERNELS_VEC4  ? v4_rpt(r)
             : f == PSV_KERNELS_FUSED ? fused_tz(r)
@@ -1479,7 +1489,7 @@ public:
                                      : rpt_ok<T>(r);
         if (f == PSV_KERNELS_TMA) by = 4;
         if (f == PSV_KERNELS_FUSED) by = (int)blk.y;  // unused
-        if (f == PSV_KERNELS_MARCH) by = march_warps(by);
+        if (f == PSV_KERNELS_MARCH) by = march_stage(by);
         if (f != PSV_KERNELS_MARCH && (by < 1 || by > 8)) by = 4;
         if (f == fam && r == rpt && (int)blk.y == by) return PSV_OK;
         fam = f;

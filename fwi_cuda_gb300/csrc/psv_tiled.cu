@@ -30,6 +30,7 @@
 
 #include "psv_kernels_impl.cuh"
 #include "psv_plan.cuh"
+#include "psv_tma.cuh"
 
 namespace psv {
 
@@ -40,7 +41,6 @@ constexpr int HX = 4;              // columns staged left and right of the tile
 constexpr int SW = TW + 2 * HX;    // staged row length (floats)
 constexpr int NTHREADS = 256;
 constexpr int NSTAGE = 2;          // tiles in flight per CTA
-constexpr unsigned WAIT_LIMIT = 1u << 20;  // try_wait rounds before giving up
 
 __host__ __device__ constexpr int halo_rows(int ns, int r) { return 4 * r + 2 * ns; }
 __host__ __device__ constexpr int halo_plane(int ns, int r) { return (halo_rows(ns, r) * SW + 31) / 32 * 32; }
@@ -65,70 +65,6 @@ template <int MODE> __host__ __device__ constexpr int vel_own_planes(bool image)
 {
     return 4 + (MODE != MODE_FWD_NOWE ? 1 : 0) + (MODE == MODE_ADJ || MODE == MODE_FWD_U ? 2 : 0) +
            (MODE == MODE_ADJ && image ? 2 : 0);
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ float *align128(unsigned char *raw)
-{
-    const uint32_t a = smem_u32(raw);
-    return reinterpret_cast<float *>(raw + ((128u - (a & 127u)) & 127u));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void fence_init()
-{
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// Orders this thread's earlier generic-proxy shared-memory accesses (after
-// the block barrier that ended the reads of a stage) before the async-proxy
-// copies that refill it.
-__device__ __forceinline__ void fence_async_smem()
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    for (unsigned n = 0; n < WAIT_LIMIT; n++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred P;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, P;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-// One box of a 3-D tensor (x = column, y = row, z = plane) into shared
-// memory; completion is signalled on `bar` as transaction bytes.
-__device__ __forceinline__ void tma_load(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
-                                         uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
 }
 
 // All threads wait (bounded) for stage barrier `bar` to complete phase
@@ -555,6 +491,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encoder()
     return encode;
 }
 
+}  // namespace
+
 // 3-D map (column, row, plane) over nplanes planes of nz x nx floats with
 // row pitch `pitch` and plane stride `plane` elements; box bx x by x 1,
 // zero fill outside.
@@ -574,8 +512,6 @@ int encode3(CUtensorMap *map, const float *base, int nx, int nz, int pitch, long
         return fail(PSV_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
     return PSV_OK;
 }
-
-}  // namespace
 
 int encode_tile_maps(TileMaps *m, const float *fld, int nfplanes, const float *coef, int nx, int nz,
                      int pitch, long long plane, int ns, int rpt)
