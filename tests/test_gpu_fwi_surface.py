@@ -40,6 +40,8 @@ FP32_STEP = 2e-2
 
 @pytest.fixture(scope="module")
 def case():
+    if not os.path.exists(FIXTURE):
+        pytest.skip("the oracle's sequence has not been generated (tests/golden/make_fwi_sequence.py)")
     z = np.load(FIXTURE)
     sv, true, init = S.surface_fwi_case()
     with engine.Plan(sv, precision=64) as p:
