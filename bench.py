@@ -683,10 +683,16 @@ def run_full_config(args):
     sigma = 15 cells, surface sources and receivers, checkpointed storage
     (two-level, or binomial with --storage binomial).
     Prints one JSON line: seconds per gradient, forward + adjoint updates/s
-    (the recomputed forward is extra work, not counted), shots/s."""
+    (the recomputed forward is extra work, not counted), shots/s.  With
+    --fwi-iterations N, then N FWI iterations from the initial model (the
+    step-length search with its trial forwards and the update included): the
+    misfit, accepted step, trial count and seconds of each.  --crop-nt M runs
+    the configuration on its first M time steps (labelled in the line)."""
     import numpy as np
     from fwi_cuda_gb300 import engine, survey as S
-    c = FULL[args.config]
+    c = dict(FULL[args.config])
+    if args.crop_nt:
+        c["nt"] = min(c["nt"], args.crop_nt)
     rng = np.random.default_rng(2024)
     fpad = c["fdorder"] // 2
     vp = S.layered_vp(c["nz"], c["nx"], c["layers"], 1500.0, 4500.0, rng, dip_cells=c["dip"],
@@ -716,8 +722,24 @@ def run_full_config(args):
         tm = p.timing()
         mem = p.device_bytes
         kind, seg, slots, adv = p.storage
+        fwi = []
+        if args.fwi_iterations:
+            p.reset_gradient()
+            step = 0.01
+            from fwi_cuda_gb300 import _lib
+            for _ in range(args.fwi_iterations):
+                t2 = time.perf_counter()
+                try:
+                    r = p.fwi_iteration(step)
+                except _lib.PSVError as e:  # a search that finds no decrease ends the run
+                    fwi.append({"error": str(e), "seconds": time.perf_counter() - t2})
+                    break
+                step = r["step"]
+                fwi.append({"L2": r["L2"], "step": step, "trials": r["ntrials"],
+                            "seconds": time.perf_counter() - t2})
     upd = 2.0 * c["nshot"] * c["nt"] * c["nz"] * c["nx"]
-    print(json.dumps({"config": args.config, "workload": {k: v for k, v in c.items()},
+    print(json.dumps({"config": args.config, "cropped_nt": bool(args.crop_nt),
+                      "fwi_iterations": fwi, "workload": {k: v for k, v in c.items()},
                       "kernels": {"family": fam, "rows_per_thread": rpt, "block_y": by},
                       "storage": {"kind": kind, "segment_steps": seg, "slots_per_shot": slots,
                                   "extra_segment_advances": adv},
@@ -777,6 +799,10 @@ def main():
                     help="run one gradient of a full configuration instead of the bench")
     ap.add_argument("--storage", choices=["checkpoint", "binomial"], default="checkpoint",
                     help="snapshot storage of the --config runs")
+    ap.add_argument("--fwi-iterations", type=int, default=0,
+                    help="with --config: FWI iterations after the gradient")
+    ap.add_argument("--crop-nt", type=int, default=0,
+                    help="with --config: run the first N time steps only")
     ap.add_argument("--slots", type=int, default=0,
                     help="state slots per shot with --storage binomial (0 = the library's choice)")
     ap.add_argument("--no-uneven", action="store_true",
