@@ -577,21 +577,23 @@ def c3_cropped(args, nt=240):
             "checkpointed_equals_full_bitwise": bool(equal), "max_rel_l2_difference": diff}
 
 
-UNEVEN = [  # (nz, nx, nt cropped, fdorder, npml, peak Hz): the uneven-batch grids, 4 shots each
+UNEVEN_SHOTS = 32
+UNEVEN = [  # (nz, nx, nt cropped, fdorder, npml, peak Hz): the uneven-batch grids
     (401, 801, 200, 4, 20, 60.0), (601, 1201, 300, 8, 30, 80.0),
     (1001, 2001, 400, 4, 30, 100.0), (1501, 3001, 600, 8, 40, 120.0)]
 
 
 def uneven_batch(args):
-    """Four surveys of the uneven-batch configuration's grid sizes (4 shots
-    each, time axes cropped to 200-600 steps, orders 4 and 8 mixed, CPML 20-40
-    cells, Ricker peaks 60-120 Hz): one FWI gradient of all four through
+    """Four surveys of the uneven-batch configuration's shape (32 shots on
+    each of its grids, 401x801 to 1501x3001, time axes cropped to 200-600
+    steps, orders 4 and 8 mixed, CPML 20-40 cells, Ricker peaks 60-120 Hz, at
+    most 40 GB of device memory each): one FWI gradient of all four through
     psv_multi_gradient (concurrent) against the same plans one after another."""
     from fwi_cuda_gb300 import engine, survey as S
     plans, pts = [], 0.0
     try:
         for k, (nz, nx, nt, fd, npml, fc) in enumerate(UNEVEN):
-            sv, true, init = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=4,
+            sv, true, init = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=UNEVEN_SHOTS,
                                               fdorder=fd, npml=npml, nrec=200, snap_dt=3,
                                               fc=fc, seed=100 + k, surf_offset=0)
             sv.imaging_sign = 1
@@ -601,7 +603,7 @@ def uneven_batch(args):
             obs = p.forward()
             p.set_model(*init)
             p.set_observed(*obs)
-            pts += 2.0 * 4 * nt * nz * nx
+            pts += 2.0 * UNEVEN_SHOTS * nt * nz * nx
         engine.multi_gradient(plans)  # tunes and captures graphs
         t0 = time.perf_counter()
         engine.multi_gradient(plans)
@@ -611,7 +613,9 @@ def uneven_batch(args):
             p.gradient(fetch=False)
         seq = time.perf_counter() - t0
         return {"workload": "4 surveys: 401x801 (nt 200), 601x1201 (300), 1001x2001 (400), "
-                            "1501x3001 (600), 4 shots each, orders 4/8, FP32",
+                            f"1501x3001 (600; cropped from 4000-12000), {UNEVEN_SHOTS} shots each, "
+                            "orders 4/8, FP32",
+                "storage": [p.storage[0] for p in plans],
                 "concurrent_s": conc, "sequential_s": seq,
                 "concurrent_updates_per_s": pts / conc, "sequential_updates_per_s": pts / seq,
                 "kernels": [dict(zip(("family", "rows_per_thread", "block_y"), p.shape)) for p in plans]}
