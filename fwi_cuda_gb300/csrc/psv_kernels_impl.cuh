@@ -69,99 +69,6 @@ __device__ __forceinline__ void cpml_stress(const StepParams<T> &p, int shot, in
     }
 }
 
-// pml_diff2 split in two for kernels that can issue the memory loads early
-// (the TMA tiles): cpml_*_load fetches the point's old strip memories,
-// cpml_*_apply performs cpml_stress's / cpml_velocity's operations with
-// them, so the results are the same bit for bit.
-template <typename T>
-struct CpmlPre {
-    T z0, z1, x0, x1;  // old memories: z-strip pair, x-strip pair (unused when off the strip)
-};
-template <typename T>
-__device__ __forceinline__ CpmlPre<T> cpml_load(const StepParams<T> &p, int shot, int iz, int ix,
-                                                int mz0, int mz1, int mx0, int mx1)
-{
-    CpmlPre<T> c{T(0), T(0), T(0), T(0)};
-    if (iz < p.pz0 || iz >= p.pz1) {
-        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-        const T *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
-        c.z0 = m[mz0 * p.mz_plane];
-        c.z1 = m[mz1 * p.mz_plane];
-    }
-    if (ix < p.px0 || ix >= p.px1) {
-        const int cc = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-        const T *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + cc;
-        c.x0 = m[mx0 * p.mx_plane];
-        c.x1 = m[mx1 * p.mx_plane];
-    }
-    return c;
-}
-template <typename T>
-__device__ __forceinline__ CpmlPre<T> cpml_stress_load(const StepParams<T> &p, int shot, int iz, int ix)
-{
-    return cpml_load(p, shot, iz, ix, MZ_VZ, MZ_VX, MX_VX, MX_VZ);
-}
-template <typename T>
-__device__ __forceinline__ CpmlPre<T> cpml_velocity_load(const StepParams<T> &p, int shot, int iz,
-                                                         int ix)
-{
-    return cpml_load(p, shot, iz, ix, MZ_SZZ, MZ_SZX, MX_SXX, MX_SZX);
-}
-// cpml_stress with the preloaded memories c.
-template <typename T>
-__device__ __forceinline__ void cpml_stress_apply(const StepParams<T> &p, int shot, int iz, int ix,
-                                                  const CpmlPre<T> &c, T &vz_z, T &vx_z, T &vz_x,
-                                                  T &vx_x)
-{
-    if (iz < p.pz0 || iz >= p.pz1) {
-        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-        T *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
-        const T m0 = p.b_z[iz] * c.z0 + p.a_z[iz] * vz_z;
-        const T m1 = p.bh_z[iz] * c.z1 + p.ah_z[iz] * vx_z;
-        m[MZ_VZ * p.mz_plane] = m0;
-        m[MZ_VX * p.mz_plane] = m1;
-        vz_z = vz_z * p.ki_z[iz] + m0;
-        vx_z = vx_z * p.khi_z[iz] + m1;
-    }
-    if (ix < p.px0 || ix >= p.px1) {
-        const int cc = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-        T *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + cc;
-        const T m0 = p.b_x[ix] * c.x0 + p.a_x[ix] * vx_x;
-        const T m1 = p.bh_x[ix] * c.x1 + p.ah_x[ix] * vz_x;
-        m[MX_VX * p.mx_plane] = m0;
-        m[MX_VZ * p.mx_plane] = m1;
-        vx_x = vx_x * p.ki_x[ix] + m0;
-        vz_x = vz_x * p.khi_x[ix] + m1;
-    }
-}
-// cpml_velocity with the preloaded memories c.
-template <typename T>
-__device__ __forceinline__ void cpml_velocity_apply(const StepParams<T> &p, int shot, int iz, int ix,
-                                                    const CpmlPre<T> &c, T &szz_z, T &szx_z,
-                                                    T &szx_x, T &sxx_x)
-{
-    if (iz < p.pz0 || iz >= p.pz1) {
-        const int rr = iz < p.pz0 ? iz : iz - p.pz1 + p.pz0;
-        T *m = p.memz + (long long)shot * p.mz_shot_stride + (long long)rr * p.pitch + ix;
-        const T m0 = p.b_z[iz] * c.z0 + p.a_z[iz] * szz_z;
-        const T m1 = p.bh_z[iz] * c.z1 + p.ah_z[iz] * szx_z;
-        m[MZ_SZZ * p.mz_plane] = m0;
-        m[MZ_SZX * p.mz_plane] = m1;
-        szz_z = szz_z * p.ki_z[iz] + m0;
-        szx_z = szx_z * p.khi_z[iz] + m1;
-    }
-    if (ix < p.px0 || ix >= p.px1) {
-        const int cc = ix < p.px0 ? ix : ix - p.px1 + p.px0;
-        T *m = p.memx + (long long)shot * p.mx_shot_stride + (long long)iz * p.mx_pitch + cc;
-        const T m0 = p.b_x[ix] * c.x0 + p.a_x[ix] * sxx_x;
-        const T m1 = p.bh_x[ix] * c.x1 + p.ah_x[ix] * szx_x;
-        m[MX_SXX * p.mx_plane] = m0;
-        m[MX_SZX * p.mx_plane] = m1;
-        sxx_x = sxx_x * p.ki_x[ix] + m0;
-        szx_x = szx_x * p.khi_x[ix] + m1;
-    }
-}
-
 // cpml_stress with ping-ponged memories (the fused families, FP32): reads
 // copy `par`, and the owner of the point writes copy 1 - par (halo points
 // only read).

@@ -131,19 +131,6 @@ __device__ __forceinline__ void stress_tile(const StepParams<float> &p, const fl
     const int x0 = T.x0, z0 = T.z0, ix = x0 + lc;
     const bool plain = T.plain;  // interior, no CPML, no free-surface row or mirror image
 
-    // Tiles on the absorbing strips: issue the strip memories' loads of all
-    // R rows before the stencil work, so their latency overlaps it.
-    CpmlPre<float> cpre[R];
-    if (!plain) {
-        const bool colin = ix >= p.nx1 && ix < p.nx2;
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int iz = z0 + lr0 + r;
-            cpre[r] = (colin && iz >= p.nz1 && iz < p.nz2) ? cpml_stress_load(p, T.bz, iz, ix)
-                                                          : CpmlPre<float>{0.f, 0.f, 0.f, 0.f};
-        }
-    }
-
     // derivatives of the thread's R rows, from shared memory only
     float dzz[R], dzx[R], dxz[R], dxx[R];  // vz_z, vz_x, vx_z, vx_x
     {
@@ -199,7 +186,7 @@ __device__ __forceinline__ void stress_tile(const StepParams<float> &p, const fl
         const long long i = (long long)iz * P + ix;
         const int k = r * TW;
         float vz_z = dzz[r], vx_z = dxz[r], vz_x = dzx[r], vx_x = dxx[r];
-        cpml_stress_apply(p, T.bz, iz, ix, cpre[r], vz_z, vx_z, vz_x, vx_x);
+        cpml_stress(p, T.bz, iz, ix, vz_z, vx_z, vz_x, vx_x);
         stress_finish(p, szz, szx, sxx, iz, ix, i, o[k], o[k + OP], o[k + 2 * OP], o[k + 3 * OP],
                       o[k + 4 * OP], o[k + 5 * OP], vz_z, vx_z, vz_x, vx_x);
     }
@@ -253,19 +240,6 @@ __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const 
     const int lc = (w & 1) * 32 + lane, lr0 = (w >> 1) * R;
     const int x0 = T.x0, z0 = T.z0, ix = x0 + lc;
     const bool plain = T.plain;  // interior, no CPML
-
-    // Tiles on the absorbing strips: the strip memories' loads of all R rows
-    // first, overlapping the stencil work.
-    CpmlPre<float> cpre[R];
-    if (!plain) {
-        const bool colin = ix >= p.nx1 && ix < p.nx2;
-#pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int iz = z0 + lr0 + r;
-            cpre[r] = (colin && iz >= p.nz1 && iz < p.nz2) ? cpml_velocity_load(p, T.bz, iz, ix)
-                                                          : CpmlPre<float>{0.f, 0.f, 0.f, 0.f};
-        }
-    }
 
     // Imaging steps: issue the history and shot-gradient loads of all R rows
     // first (they come from HBM), so their latency overlaps the stencil work.
@@ -340,7 +314,7 @@ __device__ __forceinline__ void velocity_tile(const StepParams<float> &p, const 
                                          dxxx[r], vzn, vxn, uzn, uxn);
         } else if (colin && iz >= p.nz1 && iz < p.nz2) {
             float szz_z = dzz[r], szx_z = dzxz[r], szx_x = dzxx[r], sxx_x = dxxx[r];
-            cpml_velocity_apply(p, T.bz, iz, ix, cpre[r], szz_z, szx_z, szx_x, sxx_x);
+            cpml_velocity(p, T.bz, iz, ix, szz_z, szx_z, szx_x, sxx_x);
             velocity_finish<float, MODE>(p, f, i, vzo, vxo, uzo, uxo, WE ? o[k + K_WE * OP] : 0.f,
                                          o[k + 2 * OP], o[k + 3 * OP], szz_z, szx_z, szx_x, sxx_x,
                                          vzn, vxn, uzn, uxn);
