@@ -741,6 +741,11 @@ def run_full_config(args):
                 step = r["step"]
                 fwi.append({"L2": r["L2"], "step": step, "trials": r["ntrials"],
                             "seconds": time.perf_counter() - t2})
+                # progress on stderr, so a run stopped from outside keeps its record
+                print(json.dumps({"iteration": len(fwi) - 1, **fwi[-1]}), file=sys.stderr,
+                      flush=True)
+                if args.time_budget and time.perf_counter() - t0 > args.time_budget:
+                    break
     upd = 2.0 * c["nshot"] * c["nt"] * c["nz"] * c["nx"]
     print(json.dumps({"config": args.config, "cropped_nt": bool(args.crop_nt),
                       "fwi_iterations": fwi, "workload": {k: v for k, v in c.items()},
@@ -805,6 +810,8 @@ def main():
                     help="snapshot storage of the --config runs")
     ap.add_argument("--fwi-iterations", type=int, default=0,
                     help="with --config: FWI iterations after the gradient")
+    ap.add_argument("--time-budget", type=float, default=0.0,
+                    help="with --fwi-iterations: start no iteration after this many seconds")
     ap.add_argument("--crop-nt", type=int, default=0,
                     help="with --config: run the first N time steps only")
     ap.add_argument("--slots", type=int, default=0,
