@@ -76,3 +76,14 @@ def test_roofline_byte_model_and_committed_traffic():
     assert 0 < tv < b.algorithmic_bytes("velocity_adj", 3) * updates
     assert 0 < ts < b.algorithmic_bytes("stress_adj", 3) * updates
     assert b.read_traffic("no_such_kernel") is None
+
+
+def test_step_byte_model():
+    # whole-step bytes per grid-point update behind the roofline's step
+    # fractions: 60 forward, 84 adjoint, plus the separately reported terms
+    b = _bench_module()
+    assert b.STEP_BYTES == {"forward": 60.0, "adjoint": 84.0}
+    t = b.step_terms(3)
+    assert t["forward"] == 8.0 + 20.0 / 3 and t["adjoint"] == 44.0 / 3
+    assert b.read_traffic("k_velocity_tma_adj", "dram_traffic_large.txt") == 1062.8e6
+    assert b.read_traffic("k_stress_tma_fwd", "dram_traffic_large.txt") == 528.6e6

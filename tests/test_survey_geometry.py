@@ -59,3 +59,29 @@ def test_profile_csv(tmp_path):
     np.savetxt(f, np.array([[0.0, 1.0, 2.0], [5.0, 5.5, 5.2]]).T, delimiter=",")
     x, z = S.load_profile_csv(f)
     assert list(x) == [0.0, 1.0, 2.0] and list(z) == [5.0, 5.5, 5.2]
+
+
+def test_surface_fwi_case_matches_the_configuration():
+    # the benchmark's survey: 301 x 601 cells of 0.5 m, 120 receivers every
+    # 2 m at 1 m depth, z-force Ricker sources 2 m below the surface (one
+    # shot at x = 150 m; eight shots spread along the receiver line), free
+    # surface on the first interior row with 20-cell CPML on the other sides,
+    # dt = 5e-5 s, nt = 4000, order-4 Holberg, snapshots every 3 steps
+    from fwi_cuda_gb300 import survey as S
+    sv, true, init = S.surface_fwi_case(nshot=1)
+    assert (sv.nz, sv.nx, sv.dz, sv.dx) == (301, 601, 0.5, 0.5)
+    assert (sv.nt, sv.dt, sv.fdorder, sv.stencil, sv.snap_dt) == (4000, 5e-5, 4, "holberg", 3)
+    fpad = sv.fdorder // 2
+    assert sv.surf and sv.isurf[0] == fpad and tuple(sv.npml) == (0, 20, 20, 20)
+    assert sv.nrec == 120 and np.all(np.diff(sv.x_rec) * sv.dx == 2.0)
+    assert np.all((sv.z_rec - sv.isurf[0]) * sv.dz == 1.0)
+    assert (sv.z_src[0] - sv.isurf[0]) * sv.dz == 2.0 and sv.x_src[0] * sv.dx == 150.0
+    assert np.allclose(sv.stf_x, 0.0) and np.abs(sv.stf_z).max() > 0  # vertical force
+    lam, mu, rho = true
+    vp = np.sqrt((lam + 2 * mu) / rho)
+    assert 1800 * 0.999 <= vp.min() and vp.max() <= 3000 * 1.1 * 1.001  # layers + a +10 % anomaly
+    np.testing.assert_allclose(rho, 310.0 * vp ** 0.25, rtol=1e-12)
+    np.testing.assert_allclose(np.sqrt(mu / rho), vp / 1.73, rtol=1e-12)
+    sv8, _, _ = S.surface_fwi_case(nshot=8, nt=10)
+    assert sv8.nshot == 8 and len(set(sv8.x_src)) == 8
+    assert sv8.x_src.min() >= sv8.x_rec.min() and sv8.x_src.max() <= sv8.x_rec.max()
