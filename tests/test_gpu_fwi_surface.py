@@ -13,15 +13,23 @@ gradient and model values at 2048 seeded cells after every iteration.  The
 observed data here come from the FP64 engine; they are checked against the
 oracle's norms and samples first (1e-9).
 
-Bars.  FP64 engine: identical trial counts, misfits within 1e-9, accepted
-steps within 1e-7, gradients within 1e-6 (the fixture stores the first
-gradient in float32).  FP32 engine: identical trial counts in every
-iteration (the same branches of the search), misfits within FP32_L2 and
-accepted steps within FP32_STEP of the oracle's.  An accepted step is the
-vertex of a parabola through three trial misfits, so it carries the misfit
-error divided by the parabola's relative curvature: with misfits within
-~2e-5 the steps differ by up to a few 1e-3 (measured values are printed,
-run with -s)."""
+Bars.  FP64 engine, all ten iterations: identical trial counts, misfits
+within 1e-9, accepted steps within 1e-7, gradient and model samples within
+1e-7 and 1e-9, the first gradient within 1e-6 (the fixture stores it in
+float32).
+
+FP32 engine.  Run freely, its sequence drifts from the oracle's: an accepted
+step is the vertex of a parabola through three trial misfits, so a misfit
+difference of ~1e-5 moves it by up to ~1e-2, the next model then differs by
+that much in its update, and the differences compound (measured: identical
+trial counts for five iterations, then one trial fewer at the sixth).  So
+the FP32 engine is checked iteration by iteration from the oracle's state:
+before each iteration it takes the model and the accumulated global
+gradient of the FP64 engine (which equals the oracle's to 1e-9) and runs
+one iteration, which must take the same number of trial forwards (the same
+branches of the search), a misfit within FP32_L2 and an accepted step within
+FP32_STEP of the oracle's.  The free-running FP32 sequence is printed (run
+with -s) and must end within FREE_L2 of the oracle's final misfit."""
 import os
 
 import numpy as np
@@ -36,6 +44,7 @@ pytestmark = pytest.mark.gpu
 FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "fwi_surface_301x601.npz")
 FP32_L2 = 1e-4
 FP32_STEP = 2e-2
+FREE_L2 = 2e-2
 
 
 @pytest.fixture(scope="module")
@@ -57,54 +66,66 @@ def case():
     return z, sv, init, (uz, ux)
 
 
-def _run(sv, init, obs, precision, niter):
-    rows = []
-    with engine.Plan(sv, precision=precision) as p:
-        p.set_model(*init)
-        p.set_observed(*obs)
-        step = 0.01
-        for it in range(niter):
-            r = p.fwi_iteration(step)
-            step = r["step"]
-            g = p.get_gradient()
-            m = p.get_model()
-            rows.append(dict(L2=r["L2"], step=step, ntrials=r["ntrials"], grad=g, model=m))
-    return rows
-
-
 def _sample(arrs, z):
     return np.stack([a[z["cells_z"], z["cells_x"]] for a in arrs])
 
 
-def test_fp64_engine_follows_the_oracle_sequence(gpu, case):
+def test_engine_follows_the_oracle_sequence(gpu, case):
     z, sv, init, obs = case
-    niter = 4  # the FP64 kernels are slow on this part; four iterations already cover the search's branches
-    rows = _run(sv, init, obs, 64, niter)
-    for it, r in enumerate(rows):
+    niter = int(z["niter"])
+    steps = [0.01] + list(z["step"][:-1])  # the estimate each iteration starts from
+    rows64, rows32 = [], []
+    with engine.Plan(sv, precision=64) as p64, engine.Plan(sv, precision=32) as p32:
+        for p in (p64, p32):
+            p.set_model(*init)
+            p.set_observed(*obs)
+        for it in range(niter):
+            # the FP32 iteration starts from the FP64 engine's state
+            p32.set_model(*p64.get_model())
+            p32.set_gradient(*p64.get_gradient())
+            r32 = p32.fwi_iteration(steps[it])
+            r64 = p64.fwi_iteration(steps[it])
+            rows32.append(r32)
+            rows64.append(dict(r64, grad=p64.get_gradient(), model=p64.get_model()))
+    for it, r in enumerate(rows64):
         assert r["ntrials"] == z["trials"][it], it
         assert r["L2"] == pytest.approx(z["L2"][it], rel=1e-9), it
         assert r["step"] == pytest.approx(z["step"][it], rel=1e-7), it
         assert helpers.rel_l2(_sample(r["grad"], z), z["grad_sample"][it]) < 1e-7, it
         assert helpers.rel_l2(_sample(r["model"], z), z["model_sample"][it]) < 1e-9, it
     for k in range(3):
-        assert helpers.rel_l2(rows[0]["grad"][k], z["grad_iter0"][k]) < 1e-6
-
-
-def test_fp32_engine_follows_the_oracle_sequence(gpu, case):
-    z, sv, init, obs = case
-    niter = int(z["niter"])
-    rows = _run(sv, init, obs, 32, niter)
-    e_L2 = [abs(r["L2"] - z["L2"][i]) / z["L2"][i] for i, r in enumerate(rows)]
-    e_step = [abs(r["step"] - z["step"][i]) / z["step"][i] for i, r in enumerate(rows)]
-    e_grad = [helpers.rel_l2(_sample(r["grad"], z), z["grad_sample"][i]) for i, r in enumerate(rows)]
-    print("\nFP32 vs the FP64 oracle over", niter, "iterations")
-    print("  trials  engine", [r["ntrials"] for r in rows], "oracle", list(z["trials"]))
+        assert helpers.rel_l2(rows64[0]["grad"][k], z["grad_iter0"][k]) < 1e-6
+    e_L2 = [abs(r["L2"] - z["L2"][i]) / z["L2"][i] for i, r in enumerate(rows32)]
+    e_step = [abs(r["step"] - z["step"][i]) / z["step"][i] for i, r in enumerate(rows32)]
+    print("\nFP32, each iteration from the oracle's state:")
+    print("  trials  engine", [r["ntrials"] for r in rows32], "oracle", list(z["trials"]))
     print("  misfit  rel. error", " ".join(f"{e:.1e}" for e in e_L2))
     print("  step    rel. error", " ".join(f"{e:.1e}" for e in e_step))
-    print("  gradient sample rel. L2", " ".join(f"{e:.1e}" for e in e_grad))
-    print("  first gradient rel. L2 (lam, mu, rho)",
-          " ".join(f"{helpers.rel_l2(rows[0]['grad'][k], z['grad_iter0'][k]):.1e}" for k in range(3)))
-    for it, r in enumerate(rows):
+    for it, r in enumerate(rows32):
         assert r["ntrials"] == z["trials"][it], it
     assert max(e_L2) <= FP32_L2
     assert max(e_step) <= FP32_STEP
+
+
+def test_fp32_free_running_sequence(gpu, case):
+    z, sv, init, obs = case
+    niter = int(z["niter"])
+    rows = []
+    with engine.Plan(sv, precision=32) as p:
+        p.set_model(*init)
+        p.set_observed(*obs)
+        step = 0.01
+        for it in range(niter):
+            r = p.fwi_iteration(step)
+            step = r["step"]
+            rows.append(dict(r, grad=p.get_gradient()))
+    e_L2 = [abs(r["L2"] - z["L2"][i]) / z["L2"][i] for i, r in enumerate(rows)]
+    e_step = [abs(r["step"] - z["step"][i]) / z["step"][i] for i, r in enumerate(rows)]
+    e_g0 = [helpers.rel_l2(rows[0]["grad"][k], z["grad_iter0"][k]) for k in range(3)]
+    print("\nFP32 run freely over", niter, "iterations:")
+    print("  trials  engine", [r["ntrials"] for r in rows], "oracle", list(z["trials"]))
+    print("  misfit  rel. error", " ".join(f"{e:.1e}" for e in e_L2))
+    print("  step    rel. error", " ".join(f"{e:.1e}" for e in e_step))
+    print("  first global gradient rel. L2 (lam, mu, rho)", " ".join(f"{e:.1e}" for e in e_g0))
+    assert e_L2[0] <= FP32_L2 and rows[0]["ntrials"] == z["trials"][0]
+    assert e_L2[-1] <= FREE_L2
