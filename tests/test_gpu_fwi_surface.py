@@ -22,7 +22,8 @@ FP32 engine.  Run freely, its sequence drifts from the oracle's: an accepted
 step is the vertex of a parabola through three trial misfits, so a misfit
 difference of ~1e-5 moves it by up to ~1e-2, the next model then differs by
 that much in its update, and the differences compound (measured: identical
-trial counts for five iterations, then one trial fewer at the sixth).  So
+trial counts for five iterations, then one trial fewer at the sixth; the
+final misfit 9.6e-3 from the oracle's).  So
 the FP32 engine is checked iteration by iteration from the oracle's state:
 before each iteration it takes the model and the accumulated global
 gradient of the FP64 engine (which equals the oracle's to 1e-9) and runs
@@ -42,9 +43,9 @@ from fwi_cuda_gb300 import survey as S
 pytestmark = pytest.mark.gpu
 
 FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "fwi_surface_301x601.npz")
-FP32_L2 = 1e-4
-FP32_STEP = 2e-2
-FREE_L2 = 2e-2
+FP32_L2 = 1e-4    # measured at most 2.2e-5 over the ten iterations
+FP32_STEP = 5e-3  # measured at most 1.1e-3
+FREE_L2 = 2e-2    # measured 9.6e-3 after ten free-running iterations
 
 
 @pytest.fixture(scope="module")
