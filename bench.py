@@ -588,9 +588,11 @@ def uneven_batch(args):
     each of its grids, 401x801 to 1501x3001, time axes cropped to 200-600
     steps, orders 4 and 8 mixed, CPML 20-40 cells, Ricker peaks 60-120 Hz, at
     most 40 GB of device memory each): one FWI gradient of all four through
-    psv_multi_gradient (concurrent) against the same plans one after another."""
+    psv_multi_gradient (concurrent) against the same plans one after another;
+    then forward modelling of all four concurrently, one after another and
+    in one launch per half-step (forward_modes)."""
     from fwi_cuda_gb300 import engine, survey as S
-    plans, pts = [], 0.0
+    plans, models, pts = [], [], 0.0
     try:
         for k, (nz, nx, nt, fd, npml, fc) in enumerate(UNEVEN):
             sv, true, init = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=UNEVEN_SHOTS,
@@ -599,6 +601,7 @@ def uneven_batch(args):
             sv.imaging_sign = 1
             p = engine.Plan(sv, precision=32, hbm_budget_gb=40.0, **plan_kernels(args))
             plans.append(p)
+            models.append((sv, true))
             p.set_model(*true)
             obs = p.forward()
             p.set_model(*init)
@@ -612,16 +615,69 @@ def uneven_batch(args):
         for p in plans:
             p.gradient(fetch=False)
         seq = time.perf_counter() - t0
+        kernels = [dict(zip(("family", "rows_per_thread", "block_y"), p.shape)) for p in plans]
+        storage = [p.storage[0] for p in plans]
+        for p in plans:
+            p.close()
+        # forward modelling: plans holding every shot in one batch (their
+        # history is never allocated), each with the gradient plans' tuned shape
+        plans = []
+        for (sv, true), kk in zip(models, kernels):
+            p = engine.Plan(sv, precision=32, hbm_budget_gb=250.0, max_batch=UNEVEN_SHOTS,
+                            kernels=kk["family"], rows_per_thread=kk["rows_per_thread"],
+                            block=(32, kk["block_y"]), autotune=False)
+            plans.append(p)
+            p.set_model(*true)
+        fwd = forward_modes(plans, pts / 2.0)
         return {"workload": "4 surveys: 401x801 (nt 200), 601x1201 (300), 1001x2001 (400), "
                             f"1501x3001 (600; cropped from 4000-12000), {UNEVEN_SHOTS} shots each, "
                             "orders 4/8, FP32",
-                "storage": [p.storage[0] for p in plans],
+                "storage": storage,
                 "concurrent_s": conc, "sequential_s": seq,
                 "concurrent_updates_per_s": pts / conc, "sequential_updates_per_s": pts / seq,
-                "kernels": [dict(zip(("family", "rows_per_thread", "block_y"), p.shape)) for p in plans]}
+                "kernels": kernels, "forward_modelling": fwd}
     finally:
         for p in plans:
             p.close()
+
+
+def forward_modes(plans, updates, rpt=0, by=4):
+    """Forward modelling of every survey of `plans` three ways: concurrently
+    (psv_multi_forward, each plan's own kernels), one after another, and in
+    one stress + one velocity launch per time step over all surveys
+    (psv_joint_forward: direct family, rpt rows per thread and 32 x by
+    blocks, rpt 0: the joint autotuner's shape; the plans keep that shape
+    afterwards).  Seconds per pass of all surveys (host clock around warm
+    calls; the joint pass also by CUDA events)."""
+    from fwi_cuda_gb300 import engine
+    engine.multi_forward(plans)
+    t0 = time.perf_counter()
+    engine.multi_forward(plans)
+    conc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for p in plans:
+        p.forward()
+    seq = time.perf_counter() - t0
+    out = {"concurrent_s": conc, "sequential_s": seq,
+           "concurrent_updates_per_s": updates / conc, "sequential_updates_per_s": updates / seq}
+    try:
+        with engine.Joint(plans, rows_per_thread=rpt, block_y=by) as J:
+            J.forward()  # captures the joint graph
+            t0 = time.perf_counter()
+            J.forward()
+            joint = time.perf_counter() - t0
+            jr, jb = J.shape
+            out.update(joint_s=joint, joint_device_s=J.ms * 1e-3, joint_launches=J.launches(),
+                       joint_shape={"rows_per_thread": jr, "block_y": jb},
+                       joint_updates_per_s=updates / joint)
+    except _lib_error() as e:
+        out["joint_error"] = str(e)
+    return out
+
+
+def _lib_error():
+    from fwi_cuda_gb300 import _lib
+    return _lib.PSVError
 
 
 def small_surveys(args):
@@ -629,7 +685,8 @@ def small_surveys(args):
     each): one FWI gradient of all eight through psv_multi_gradient (one
     stream per survey), one after another, and one survey holding all 16
     shots (one launch per half-step: the most a single launch over the eight
-    surveys could reach)."""
+    surveys could reach); then forward modelling the same ways and through
+    the joint launch over the eight surveys (forward_modes)."""
     from fwi_cuda_gb300 import engine, survey as S
     plans = []
 
@@ -647,9 +704,9 @@ def small_surveys(args):
 
     try:
         each = [plan(2, 200 + k) for k in range(8)]
-        joint = plan(16, 300)
+        one16 = plan(16, 300)
         engine.multi_gradient(each)  # tunes and captures graphs
-        joint.gradient(fetch=False)
+        one16.gradient(fetch=False)
         t0 = time.perf_counter()
         engine.multi_gradient(each)
         conc = time.perf_counter() - t0
@@ -658,13 +715,20 @@ def small_surveys(args):
             p.gradient(fetch=False)
         seq = time.perf_counter() - t0
         t0 = time.perf_counter()
-        joint.gradient(fetch=False)
+        one16.gradient(fetch=False)
         one = time.perf_counter() - t0
         upd = 2.0 * 16 * 500 * 101 * 201
+        one16.forward()
+        t0 = time.perf_counter()
+        one16.forward()
+        one_fwd = time.perf_counter() - t0
+        fwd = forward_modes(each, upd / 2.0)
+        fwd["one_survey_16_shots_s"] = one_fwd
+        fwd["one_survey_updates_per_s"] = upd / 2.0 / one_fwd
         return {"workload": "8 surveys of 101x201, 2 shots each, nt 500, order 4, FP32",
                 "concurrent_s": conc, "sequential_s": seq, "one_survey_16_shots_s": one,
                 "concurrent_updates_per_s": upd / conc, "sequential_updates_per_s": upd / seq,
-                "one_survey_updates_per_s": upd / one}
+                "one_survey_updates_per_s": upd / one, "forward_modelling": fwd}
     finally:
         for p in plans:
             p.close()

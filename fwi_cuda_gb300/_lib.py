@@ -114,6 +114,12 @@ SIGNATURES = {
                                           C.POINTER(C.c_longlong)]),
     "psv_multi_forward": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(_dp), C.POINTER(_dp)]),
     "psv_multi_gradient": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, _dp]),
+    "psv_joint_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
+                                   C.POINTER(C.c_void_p)]),
+    "psv_joint_forward": (C.c_int, [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), _dp]),
+    "psv_joint_launches": (C.c_longlong, [C.c_void_p]),
+    "psv_joint_shape": (C.c_int, [C.c_void_p, _ip, _ip]),
+    "psv_joint_destroy": (C.c_int, [C.c_void_p]),
     "psv_step_length": (C.c_int, [_dp, C.c_double, C.c_void_p, C.c_void_p, _ip, _dp, C.c_int]),
     "psv_calc_opt_step": (C.c_double, [_dp, _dp]),
     "psv_kernel_PSV": (C.c_int,

@@ -37,6 +37,7 @@ UNITS = [
     ("psv_fused.cu", []),
     ("psv_march.cu", []),
     ("psv_exact.cu", []),
+    ("psv_joint.cu", []),
     ("psv_fwi_kernels.cu", ["-fmad=false"]),
     ("psv_plan_f32.cu", []),
     ("psv_plan_f64.cu", []),

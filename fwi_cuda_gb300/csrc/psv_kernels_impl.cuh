@@ -587,12 +587,13 @@ __device__ __forceinline__ void stress_rows_inner(const StepParams<T> &p, T *f, 
 // ---------------------------------------------------------------------------
 // Stress step, direct loads: vdiff2 + pml_diff2 + update_s2 + surf_mirror
 // (src/cpu/n_kernel_lib_PSV.cpp:100-131, 134-205, 272-395).  Interior points
-// only.
+// only.  stress_block is one block's work (block bp of a grid over the
+// interior, 32 x blockDim.y threads); k_stress runs it over one survey's
+// batch, k_joint_stress over several surveys (psv_joint.cu).
 // ---------------------------------------------------------------------------
 template <typename T, int NS, int RPT, bool SH>
-__global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
+__device__ __forceinline__ void stress_block(const StepParams<T> &p, const BlockPos bp)
 {
-    const BlockPos bp = block_pos(p.nbatch);
     if (bp.bz >= p.ctl[1]) return;
     const int ix = p.nx1 + bp.bx * 32 + threadIdx.x;
     const int zb = p.nz1 + (bp.by * blockDim.y + threadIdx.y) * RPT;
@@ -656,6 +657,12 @@ __global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
         stress_finish(p, szz, szx, sxx, iz, ix, i, szz[i], szx[i], sxx[i], p.c_lam[i], p.c_l2m[i],
                       p.c_muzx[i], vz_z, vx_z, vz_x, vx_x);
     }
+}
+
+template <typename T, int NS, int RPT, bool SH>
+__global__ void __launch_bounds__(256) k_stress(const StepParams<T> p)
+{
+    stress_block<T, NS, RPT, SH>(p, block_pos(p.nbatch));
 }
 
 // Velocity update (with the step's snapshot store / imaging) of rows
@@ -724,13 +731,15 @@ __device__ __forceinline__ void velocity_rows_inner(const StepParams<T> &p, T *f
 //   epilogue: vsrc2 + urec2 (:487-576) for the sources / receivers of the
 //   block's tile, after all of the tile's velocities are written.
 // Covers the whole grid: cells outside the interior only take part in the
-// snapshot / imaging work (their fields are never updated).
+// snapshot / imaging work (their fields are never updated).  velocity_block
+// is one block's work (block bp of a grid over the whole nz x nx plane);
+// k_velocity runs it over one survey's batch, k_joint_velocity over several
+// surveys (psv_joint.cu).
 // ---------------------------------------------------------------------------
 template <typename T, int NS, int MODE, int RPT, bool SH>
-__global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const SrcRecParams<T> q,
-                                                  const int it, const int slot)
+__device__ __forceinline__ void velocity_block(const StepParams<T> &p, const SrcRecParams<T> &q,
+                                               const int it, const int slot, const BlockPos bp)
 {
-    const BlockPos bp = block_pos(p.nbatch);
     if (bp.bz >= p.ctl[1]) return;  // whole block
     const int ix = bp.bx * 32 + threadIdx.x;
     const int zb = (bp.by * blockDim.y + threadIdx.y) * RPT;
@@ -814,6 +823,13 @@ __global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const S
     }
     srcrec_tile<T, MODE>(p, q, it, slot, bp.by * bp.ntx + bp.bx, bp.bz,
                          threadIdx.y * 32 + threadIdx.x, 32 * blockDim.y);
+}
+
+template <typename T, int NS, int MODE, int RPT, bool SH>
+__global__ void __launch_bounds__(256) k_velocity(const StepParams<T> p, const SrcRecParams<T> q,
+                                                  const int it, const int slot)
+{
+    velocity_block<T, NS, MODE, RPT, SH>(p, q, it, slot, block_pos(p.nbatch));
 }
 
 // ---------------------------------------------------------------------------

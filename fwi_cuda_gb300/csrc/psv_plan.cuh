@@ -98,6 +98,21 @@ cudaError_t launch_exact_adjoint_step(const StepParams<double> &p, const SrcRecP
 cudaError_t launch_exact_chain(const StepParams<double> &p, const ExactBufs &X, const double *lam,
                                const double *mu, const double *rho, double *gl, double *gm,
                                double *gr, double dt, double sign, cudaStream_t st);
+// Joint launches over several surveys (psv_joint.cu): one stress and one
+// velocity launch per time step cover every shot of up to JOINT_MAX surveys
+// of any grid size, stencil order and step count, the direct family's block
+// bodies with one tile shape.  A survey's entry: its plan's step and forward
+// source / receiver parameters, stencil terms, step count, and the blocks of
+// its stress (interior) and velocity (whole plane) grids per shot.
+constexpr int JOINT_MAX = 8;
+template <typename T>
+struct JointSurvey {
+    StepParams<T> p;
+    SrcRecParams<T> q;
+    int ns, nt, nb;  // stencil terms, time steps, shots
+    int sx, sy;      // stress grid blocks along x and z
+    int vx, vy;      // velocity grid blocks along x and z
+};
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
 cudaError_t launch_velocity_tma(const StepParams<float> &p, const SrcRecParams<float> &q,
@@ -169,6 +184,7 @@ struct DevMem {
 struct PlanIface {
     virtual ~PlanIface() = default;
     virtual long long device_bytes() const = 0;
+    virtual int precision() const = 0;  // 32 or 64: the wavefields' floating-point width
     virtual int set_model(const double *lam, const double *mu, const double *rho) = 0;
     virtual int get_model(double *lam, double *mu, double *rho) = 0;
     virtual int set_observed(const double *uz, const double *ux) = 0;
@@ -194,6 +210,12 @@ struct PlanIface {
     virtual void storage(int *kind, int *segment_steps, int *slots, long long *advances) const = 0;
     virtual int chain_count() const = 0;
     virtual int prepare() = 0;  // history buffers and the pending autotune, before concurrent use
+    // Joint forward modelling (psv_joint.cu): switch to the direct family with
+    // rpt rows per thread and 32 x by blocks, zero the wavefields, fill the
+    // JointSurvey<T> at `entry` (`bytes` = its size: the precisions agree);
+    // after the joint time loop, fetch the traces.
+    virtual int joint_begin(int rpt, int by, void *entry, size_t bytes) = 0;
+    virtual int joint_end(double *rtf_uz, double *rtf_ux) = 0;
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
                             const double *rho_zp, const double *rho_xp, int ishot, int grad,

@@ -1615,6 +1615,45 @@ public:
         return maybe_autotune();
     }
 
+    int joint_begin(int r, int by, void *entry, size_t bytes) override
+    {
+        if (bytes != sizeof(JointSurvey<T>))
+            return fail(PSV_ERR_ARG, "joint launch: every plan of one precision");
+        if (!have_model) return fail(PSV_ERR_ARG, "joint launch: a plan has no model");
+        if (nbatch != 1)
+            return fail(PSV_ERR_UNSUPPORTED, "joint launch: every shot of a survey in one batch "
+                                             "(max_batch >= nshot)");
+        PSV_TRY(set_shape(PSV_KERNELS_DIRECT, r, by));
+        if (fam != PSV_KERNELS_DIRECT || rpt != r || (int)blk.y != by)
+            return fail(PSV_ERR_ARG, "joint launch: unsupported tile shape");
+        PSV_TRY(set_batch(0));
+        // reset_sv2 / reset_PML_memory2 (n_kernel_PSV.cpp:74-88), as the plain forward pass
+        T *f = fld.as<T>();
+        PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
+        PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+        PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+        JointSurvey<T> &e = *static_cast<JointSurvey<T> *>(entry);
+        e.p = sp;
+        e.q = qf;
+        e.ns = sv.ns;
+        e.nt = sv.g.nt;
+        e.nb = B;
+        const int tz = by * r;
+        e.sx = (sv.nx2 - sv.nx1 + 31) / 32;
+        e.sy = (sv.nz2 - sv.nz1 + tz - 1) / tz;
+        e.vx = (sv.g.nx + 31) / 32;
+        e.vy = (sv.g.nz + tz - 1) / tz;
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    int joint_end(double *uz, double *ux) override
+    {
+        if (uz && sv.s.nrec) PSV_TRY(download_traces(uz, tr(0), 0, sv.s.nshot));
+        if (ux && sv.s.nrec) PSV_TRY(download_traces(ux, tr(1), 0, sv.s.nshot));
+        return sync_check();
+    }
+
     int maybe_autotune()
     {
         if (tuned || !opt.autotune || !have_model || !have_obs) return PSV_OK;
@@ -1622,6 +1661,7 @@ public:
     }
 
     void *stream() const override { return (void *)st; }
+    int precision() const override { return (int)sizeof(T) * 8; }
     long long launches() const override { return nlaunch; }
 
     // Per-kernel event timing of nsteps forward then nsteps adjoint steps.

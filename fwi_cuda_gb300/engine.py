@@ -340,6 +340,68 @@ def multi_forward(plans):
     return out
 
 
+class Joint:
+    """psv_joint_*: forward modelling of up to 8 surveys (one Plan each, one
+    precision, every shot in one batch) in one stress and one velocity
+    launch per time step; grid sizes, stencil orders, shot and step counts
+    may differ.  The plans run the direct kernel family with the joint tile
+    shape (rows_per_thread x 32 x block_y threads; rows_per_thread 0: chosen
+    by timing the first steps on the first forward)."""
+
+    def __init__(self, plans, rows_per_thread=0, block_y=4):
+        self.plans = list(plans)
+        n = len(self.plans)
+        self._hs = (C.c_void_p * n)(*[p.h for p in self.plans])
+        self.h = C.c_void_p()
+        check(_lib.lib().psv_joint_create(self._hs, n, int(rows_per_thread), int(block_y),
+                                          C.byref(self.h)))
+        self.ms = 0.0
+
+    def forward(self, fetch=True):
+        """One joint pass; returns [(uz, ux)] per plan ([] with fetch=False).
+        self.ms holds the device time of the joint time loop."""
+        n = len(self.plans)
+        out = []
+        uz = ux = None
+        if fetch:
+            out = [(np.zeros((p.sv.nshot, p.sv.nrec, p.sv.nt)), np.zeros((p.sv.nshot, p.sv.nrec, p.sv.nt)))
+                   for p in self.plans]
+            uz = (_lib._dp * n)(*[dptr(o[0]) for o in out])
+            ux = (_lib._dp * n)(*[dptr(o[1]) for o in out])
+        ms = np.zeros(1)
+        check(_lib.lib().psv_joint_forward(self.h, uz, ux, dptr(ms)))
+        self.ms = float(ms[0])
+        return out
+
+    def launches(self) -> int:
+        return int(_lib.lib().psv_joint_launches(self.h))
+
+    @property
+    def shape(self):
+        """(rows_per_thread, block_y) of the joint launches ((0, 0) before an
+        autotuning first forward)."""
+        r, b = np.zeros(1, np.int32), np.zeros(1, np.int32)
+        check(_lib.lib().psv_joint_shape(self.h, iptr(r), iptr(b)))
+        return int(r[0]), int(b[0])
+
+    def close(self):
+        if self.h:
+            _lib.lib().psv_joint_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 def multi_gradient(plans):
     """psv_multi_gradient: one FWI gradient of every survey (one Plan each)
     concurrently; returns L2 per plan, gradients stay on the plans."""

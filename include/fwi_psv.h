@@ -241,6 +241,44 @@ int psv_gradient(psv_plan *plan, double *L2, double *grad_lam, double *grad_mu,
 int psv_multi_forward(psv_plan *const *plans, int nplans, double *const *rtf_uz,
                       double *const *rtf_ux);
 int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
+
+/* Joint forward modelling: up to 8 surveys (one plan each, all of one
+ * precision, every shot of a plan in one batch: max_batch >= nshot) stepped
+ * in ONE stress launch and ONE velocity launch per time step, whose blocks
+ * cover every shot of every survey still running.  Grid sizes, stencil
+ * orders (mixed in one launch), shot counts and step counts may differ; a
+ * survey leaves the launches after its last step.  The time loop is one
+ * CUDA graph, captured by the first psv_joint_forward and replayed by the
+ * later ones.
+ *   psv_joint_create: the plans and the tile shape of the joint launches
+ *     (rows_per_thread 1, 2 or 4, FP64: 1; blocks of 32 x block_y threads,
+ *     block_y 1..8), or rows_per_thread 0: the first psv_joint_forward
+ *     times the first steps (up to 24) of the joint loop for each of a few
+ *     shapes and keeps the fastest.  Every psv_joint_forward sets each plan
+ *     to the direct kernel family with the joint shape (psv_plan_shape
+ *     reports it; the plan's own passes then use it too).
+ *   psv_joint_shape: the joint shape (0, 0 while an autotune is pending).
+ *   psv_joint_forward: psv_forward of every plan (uz[k], ux[k] as there;
+ *     NULL arrays or entries skip the download); *ms (may be NULL) gets the
+ *     device time of the joint time loop.  The operations per grid point are
+ *     those of each plan's own psv_forward with the same tile shape; the
+ *     joint kernels' compiled multiply-add contraction may differ, so traces
+ *     agree to rounding (FP32 relative L2 ~1e-8), not bit for bit.  One
+ *     joint pass runs at a time per process (the survey tables are in
+ *     constant memory).
+ *   psv_joint_launches: kernel launches of one psv_joint_forward (2 x the
+ *     longest step count; 0 before the first call).
+ * Errors: PSV_ERR_ARG (more than 8 plans, mixed precisions, a plan twice,
+ * no model), PSV_ERR_UNSUPPORTED (a plan with more than one batch).  No
+ * counterpart in the reference (one survey per program run). */
+typedef struct psv_joint psv_joint;
+int psv_joint_create(psv_plan *const *plans, int nplans, int rows_per_thread, int block_y,
+                     psv_joint **out);
+int psv_joint_forward(psv_joint *joint, double *const *rtf_uz, double *const *rtf_ux, double *ms);
+long long psv_joint_launches(const psv_joint *joint);
+int psv_joint_shape(const psv_joint *joint, int *rows_per_thread, int *block_y);
+int psv_joint_destroy(psv_joint *joint);
+
 int psv_reset_gradient(psv_plan *plan);
 int psv_get_gradient(psv_plan *plan, double *grad_lam, double *grad_mu, double *grad_rho);
 int psv_set_gradient(psv_plan *plan, const double *grad_lam, const double *grad_mu,

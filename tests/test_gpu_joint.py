@@ -1,0 +1,151 @@
+"""Joint forward modelling (psv_joint_*, psv_joint.cu): several surveys of
+uneven grid size, shot count, step count and stencil order stepped in one
+stress and one velocity launch per time step must give each survey's own
+traces (the same block bodies as the plan's direct launches with the same
+tile shape) to rounding: relative L2 <= 1e-6 in FP32 (the joint kernels'
+compiled multiply-add contraction may differ from the single-survey
+kernels'), <= 1e-12 in FP64; repeated calls (graph replays) must repeat
+themselves bit for bit, and the traces match the FP64 oracle."""
+import numpy as np
+import pytest
+
+import helpers
+from fwi_cuda_gb300 import _lib, engine
+
+pytestmark = pytest.mark.gpu
+
+CASES = [dict(fdorder=4, nz=61, nx=91, nt=300, nshot=2),                       # mirrored rows above the surface
+         dict(fdorder=8, nz=83, nx=157, nt=220, nshot=3, surf_offset=0),       # surface on the first interior row
+         dict(fdorder=2, stencil="reference", nz=50, nx=70, nt=350, nshot=1),
+         dict(fdorder=6, nz=47, nx=133, nt=260, nshot=2, snap_dt=3)]
+
+
+def _surveys():
+    out = []
+    for kw in CASES:
+        kw = dict(dict(stencil="holberg"), **kw)
+        out.append(helpers.case(**kw))
+    sv, true, init = helpers.crosswell(nt=280, nshot=2)  # CPML on four sides, x-force sources
+    out.append((sv, true, init))
+    return out
+
+
+def _shape(precision, rpt, by):
+    return dict(precision=precision, kernels="direct", rows_per_thread=rpt, block=(32, by),
+                autotune=False)
+
+
+def _separate(surveys, **shape):
+    res = []
+    for sv, true, _ in surveys:
+        with engine.Plan(sv, **shape) as p:
+            p.set_model(*true)
+            res.append(p.forward())
+    return res
+
+
+@pytest.mark.parametrize("precision,rpt,by", [(32, 1, 4), (32, 2, 4), (32, 4, 2), (64, 1, 8)])
+def test_joint_forward_equals_each_plan(gpu, precision, rpt, by):
+    surveys = _surveys()
+    shape = _shape(precision, rpt, by)
+    ref = _separate(surveys, **shape)
+    plans = [engine.Plan(sv, **shape) for sv, *_ in surveys]
+    try:
+        for p, (sv, true, _) in zip(plans, surveys):
+            p.set_model(*true)
+        bar = 1e-6 if precision == 32 else 1e-12
+        with engine.Joint(plans, rows_per_thread=rpt, block_y=by) as J:
+            first = J.forward()
+            again = J.forward()  # replays the captured graph
+            assert J.launches() == 2 * max(sv.nt for sv, *_ in surveys)
+            assert J.ms > 0
+        err = []
+        for k, ((uz, ux), (az, ax), (rz, rx)) in enumerate(zip(first, again, ref)):
+            assert np.array_equal(uz, az) and np.array_equal(ux, ax), k
+            err.append(max(helpers.rel_l2(uz, rz), helpers.rel_l2(ux, rx)))
+        print(f"\nFP{precision} rpt {rpt} by {by}: joint vs each plan, rel. L2 per survey",
+              " ".join(f"{e:.1e}" for e in err))
+        assert max(err) <= bar
+        # the plans' own passes afterwards are unaffected
+        for p, (rz, rx) in zip(plans, ref):
+            uz, ux = p.forward()
+            assert np.array_equal(uz, rz) and np.array_equal(ux, rx)
+    finally:
+        for p in plans:
+            p.close()
+
+
+def test_joint_forward_against_oracle(gpu, orc):
+    surveys = _surveys()[:3]
+    plans = [engine.Plan(sv, **_shape(32, 1, 4)) for sv, *_ in surveys]
+    try:
+        for p, (sv, true, _) in zip(plans, surveys):
+            p.set_model(*true)
+        with engine.Joint(plans) as J:  # shape autotuned on the first forward
+            assert J.shape == (0, 0)
+            out = J.forward()
+            r, b = J.shape
+            assert r in (1, 2, 4) and b in (2, 4, 8)
+            assert all(p.shape == ("direct", r, b) for p in plans)
+        for (uz, ux), (sv, true, _) in zip(out, surveys):
+            rz, rx = orc.simulate_fwd(sv, *true)
+            assert helpers.rel_l2(uz, rz) < 1e-5 and helpers.rel_l2(ux, rx) < 1e-5
+    finally:
+        for p in plans:
+            p.close()
+
+
+def test_joint_switches_autotuned_plans_to_its_shape(gpu):
+    # plans created with the default options (any family) are set to the
+    # direct family with the joint shape and give that shape's traces
+    surveys = _surveys()[:2]
+    ref = _separate(surveys, **_shape(32, 2, 4))
+    plans = [engine.Plan(sv, precision=32) for sv, *_ in surveys]
+    try:
+        for p, (sv, true, _) in zip(plans, surveys):
+            p.set_model(*true)
+        with engine.Joint(plans, rows_per_thread=2, block_y=4) as J:
+            out = J.forward()
+        for p, (uz, ux), (rz, rx) in zip(plans, out, ref):
+            assert p.shape == ("direct", 2, 4)
+            assert helpers.rel_l2(uz, rz) <= 1e-6 and helpers.rel_l2(ux, rx) <= 1e-6
+            fz, fx = p.forward()  # the plan's own pass now has the joint shape
+            assert np.array_equal(fz, rz) and np.array_equal(fx, rx)
+    finally:
+        for p in plans:
+            p.close()
+
+
+def test_joint_rejects_what_it_does_not_run(gpu):
+    s = _surveys()
+    a = engine.Plan(s[0][0], precision=32)
+    b = engine.Plan(s[1][0], precision=64)
+    c = engine.Plan(s[1][0], precision=32, max_batch=1)  # three shots, one per batch
+    try:
+        for p, k in ((a, 0), (b, 1), (c, 1)):
+            p.set_model(*s[k][1])
+        with pytest.raises(_lib.PSVError, match="precision"):
+            engine.Joint([a, b])
+        with pytest.raises(_lib.PSVError, match="twice"):
+            engine.Joint([a, a])
+        with pytest.raises(_lib.PSVError, match="1 to 8"):
+            engine.Joint([])
+        with pytest.raises(_lib.PSVError, match="rows_per_thread"):
+            engine.Joint([a], rows_per_thread=3)
+        with pytest.raises(_lib.PSVError, match="block_y"):
+            engine.Joint([a], rows_per_thread=1, block_y=9)
+        with pytest.raises(_lib.PSVError, match="FP64"):
+            engine.Joint([b], rows_per_thread=2)
+        with engine.Joint([a, c], rows_per_thread=1) as J:
+            with pytest.raises(_lib.PSVError, match="one batch"):
+                J.forward()
+        d = engine.Plan(s[2][0], precision=32)  # no model
+        try:
+            with engine.Joint([a, d], rows_per_thread=1) as J:
+                with pytest.raises(_lib.PSVError, match="no model"):
+                    J.forward()
+        finally:
+            d.close()
+    finally:
+        for p in (a, b, c):
+            p.close()
