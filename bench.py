@@ -686,7 +686,8 @@ def small_surveys(args):
     stream per survey), one after another, and one survey holding all 16
     shots (one launch per half-step: the most a single launch over the eight
     surveys could reach); then forward modelling the same ways and through
-    the joint launch over the eight surveys (forward_modes)."""
+    the joint launch over the eight surveys (forward_modes), and the
+    gradient of all eight through the joint passes."""
     from fwi_cuda_gb300 import engine, survey as S
     plans = []
 
@@ -725,10 +726,25 @@ def small_surveys(args):
         fwd = forward_modes(each, upd / 2.0)
         fwd["one_survey_16_shots_s"] = one_fwd
         fwd["one_survey_updates_per_s"] = upd / 2.0 / one_fwd
-        return {"workload": "8 surveys of 101x201, 2 shots each, nt 500, order 4, FP32",
-                "concurrent_s": conc, "sequential_s": seq, "one_survey_16_shots_s": one,
-                "concurrent_updates_per_s": upd / conc, "sequential_updates_per_s": upd / seq,
-                "one_survey_updates_per_s": upd / one, "forward_modelling": fwd}
+        out = {"workload": "8 surveys of 101x201, 2 shots each, nt 500, order 4, FP32",
+               "concurrent_s": conc, "sequential_s": seq, "one_survey_16_shots_s": one,
+               "concurrent_updates_per_s": upd / conc, "sequential_updates_per_s": upd / seq,
+               "one_survey_updates_per_s": upd / one, "forward_modelling": fwd}
+        # the gradient of all eight through the joint passes (autotuned shape)
+        try:
+            with engine.Joint(each) as J:
+                J.gradient()  # tunes and captures the passes
+                for p in each:
+                    p.reset_gradient()
+                t0 = time.perf_counter()
+                J.gradient()
+                jg = time.perf_counter() - t0
+                jr, jb = J.shape
+                out.update(joint_s=jg, joint_device_s=J.ms * 1e-3, joint_updates_per_s=upd / jg,
+                           joint_shape={"rows_per_thread": jr, "block_y": jb})
+        except _lib_error() as e:
+            out["joint_error"] = str(e)
+        return out
     finally:
         for p in plans:
             p.close()

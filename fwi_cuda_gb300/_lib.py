@@ -117,6 +117,7 @@ SIGNATURES = {
     "psv_joint_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int,
                                    C.POINTER(C.c_void_p)]),
     "psv_joint_forward": (C.c_int, [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), _dp]),
+    "psv_joint_gradient": (C.c_int, [C.c_void_p, _dp, _dp]),
     "psv_joint_launches": (C.c_longlong, [C.c_void_p]),
     "psv_joint_shape": (C.c_int, [C.c_void_p, _ip, _ip]),
     "psv_joint_destroy": (C.c_int, [C.c_void_p]),

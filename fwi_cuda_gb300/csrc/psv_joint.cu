@@ -1,5 +1,5 @@
-// psv_joint.cu -- forward modelling of several surveys in one launch per
-// half-step.
+// psv_joint.cu -- forward modelling and FWI gradients of several surveys in
+// one launch per half-step.
 //
 // A joint pass steps up to JOINT_MAX surveys (one plan each: any grid size,
 // stencil order, step count and shot count) together: every time step is one
@@ -20,7 +20,15 @@
 // into segments; segment g holds the surveys with more than its first step
 // (their order and first blocks in c_seg[g]).  A survey leaves the launches
 // after its last step.  The whole loop (2 x the longest step count launches)
-// is one CUDA graph, captured once per joint object and replayed per call.
+// is one CUDA graph per velocity mode, captured once per joint object and
+// replayed per call.
+//
+// Gradient (psv_joint_gradient, full snapshot storage): the gradient forward
+// pass (MODE_FWD, snapshots every sdt-th step) and the adjoint pass
+// (MODE_ADJ, imaging) each run jointly; at joint step k a survey runs its own
+// step k, or nt - 1 - k in the time-reversed adjoint pass, with its own
+// snapshot slot.  Residuals, adjoint sources and preconditioning run per plan
+// between and after the passes (PlanIface::joint_gradient_phase).
 #include <algorithm>
 #include <mutex>
 #include <numeric>
@@ -71,8 +79,9 @@ __device__ __forceinline__ BlockPos joint_pos(int b, int gx, int gy)
     return {b / (gx * gy), b % gx, (b / gx) % gy, gx};
 }
 
-// The block bodies of stencil half-widths 1 .. NSMAX (the largest among the
-// joint surveys): the kernel's registers are those of the widest body present.
+// The block bodies of stencil half-widths 1 .. NSMAX (2 or 4: the widest
+// among the joint surveys), so surveys of orders up to 4 do not pay the
+// registers of the order-8 body.
 template <typename T, int RPT, int NSMAX>
 __global__ void __launch_bounds__(256) k_joint_stress(const int g)
 {
@@ -80,63 +89,64 @@ __global__ void __launch_bounds__(256) k_joint_stress(const int g)
     const int j = joint_slot(sg.s0, sg.n, (int)blockIdx.x);
     const JointSurvey<T> &e = joint_entry<T>(sg.idx[j]);
     const BlockPos bp = joint_pos((int)blockIdx.x - sg.s0[j], e.sx, e.sy);
-    if constexpr (NSMAX >= 4)
+    if constexpr (NSMAX >= 4) {
         if (e.ns == 4) return stress_block<T, 4, RPT, false>(e.p, bp);
-    if constexpr (NSMAX >= 3)
         if (e.ns == 3) return stress_block<T, 3, RPT, false>(e.p, bp);
-    if constexpr (NSMAX >= 2)
-        if (e.ns == 2) return stress_block<T, 2, RPT, false>(e.p, bp);
+    }
+    if (e.ns == 2) return stress_block<T, 2, RPT, false>(e.p, bp);
     stress_block<T, 1, RPT, false>(e.p, bp);
 }
 
-// Plain forward step (MODE_FWD_NOWE): sources and receivers, no snapshots.
-template <typename T, int RPT, int NSMAX>
-__global__ void __launch_bounds__(256) k_joint_velocity(const int g, const int it)
+// Velocity step of mode MODE (MODE_FWD_NOWE: forward modelling; MODE_FWD:
+// the gradient's forward pass with snapshots; MODE_ADJ: the adjoint pass
+// with imaging) at joint step k: the survey's own step it (k, or nt - 1 - k
+// in the time-reversed pass) and snapshot slot.
+template <typename T, int RPT, int NSMAX, int MODE>
+__global__ void __launch_bounds__(256) k_joint_velocity(const int g, const int k)
 {
     const JointSeg &sg = c_seg[g];
     const int j = joint_slot(sg.v0, sg.n, (int)blockIdx.x);
     const JointSurvey<T> &e = joint_entry<T>(sg.idx[j]);
     const BlockPos bp = joint_pos((int)blockIdx.x - sg.v0[j], e.vx, e.vy);
-    constexpr int M = MODE_FWD_NOWE;
-    if constexpr (NSMAX >= 4)
-        if (e.ns == 4) return velocity_block<T, 4, M, RPT, false>(e.p, e.q, it, -1, bp);
-    if constexpr (NSMAX >= 3)
-        if (e.ns == 3) return velocity_block<T, 3, M, RPT, false>(e.p, e.q, it, -1, bp);
-    if constexpr (NSMAX >= 2)
-        if (e.ns == 2) return velocity_block<T, 2, M, RPT, false>(e.p, e.q, it, -1, bp);
-    velocity_block<T, 1, M, RPT, false>(e.p, e.q, it, -1, bp);
+    const int it = e.rev ? e.nt - 1 - k : k;
+    const int slot = (e.sdt > 0 && !(it % e.sdt)) ? (it / e.sdt) % e.ring : -1;
+    if constexpr (NSMAX >= 4) {
+        if (e.ns == 4) return velocity_block<T, 4, MODE, RPT, false>(e.p, e.q, it, slot, bp);
+        if (e.ns == 3) return velocity_block<T, 3, MODE, RPT, false>(e.p, e.q, it, slot, bp);
+    }
+    if (e.ns == 2) return velocity_block<T, 2, MODE, RPT, false>(e.p, e.q, it, slot, bp);
+    velocity_block<T, 1, MODE, RPT, false>(e.p, e.q, it, slot, bp);
 }
 
 template <typename T, int RPT, int NSMAX>
-void joint_pair(int g, int it, int sblocks, int vblocks, int by, cudaStream_t st)
+void joint_pair(int g, int k, int sblocks, int vblocks, int by, int mode, cudaStream_t st)
 {
     const dim3 blk(32, by, 1);
     k_joint_stress<T, RPT, NSMAX><<<sblocks, blk, 0, st>>>(g);
-    k_joint_velocity<T, RPT, NSMAX><<<vblocks, blk, 0, st>>>(g, it);
+    if (mode == MODE_FWD) k_joint_velocity<T, RPT, NSMAX, MODE_FWD><<<vblocks, blk, 0, st>>>(g, k);
+    else if (mode == MODE_ADJ) k_joint_velocity<T, RPT, NSMAX, MODE_ADJ><<<vblocks, blk, 0, st>>>(g, k);
+    else k_joint_velocity<T, RPT, NSMAX, MODE_FWD_NOWE><<<vblocks, blk, 0, st>>>(g, k);
 }
 
 template <typename T, int RPT>
-void joint_pair_r(int g, int it, int sblocks, int vblocks, int by, int nsmax, cudaStream_t st)
+void joint_pair_r(int g, int k, int sblocks, int vblocks, int by, int nsmax, int mode, cudaStream_t st)
 {
-    switch (nsmax) {
-    case 1: joint_pair<T, RPT, 1>(g, it, sblocks, vblocks, by, st); break;
-    case 2: joint_pair<T, RPT, 2>(g, it, sblocks, vblocks, by, st); break;
-    case 3: joint_pair<T, RPT, 3>(g, it, sblocks, vblocks, by, st); break;
-    default: joint_pair<T, RPT, 4>(g, it, sblocks, vblocks, by, st); break;
-    }
+    if (nsmax <= 2) joint_pair<T, RPT, 2>(g, k, sblocks, vblocks, by, mode, st);
+    else joint_pair<T, RPT, 4>(g, k, sblocks, vblocks, by, mode, st);
 }
 
+// One joint time step k of segment g (mode: MODE_FWD_NOWE, MODE_FWD or MODE_ADJ).
 template <typename T>
-cudaError_t launch_joint_step(int g, int it, int sblocks, int vblocks, int rpt, int by, int nsmax,
-                              cudaStream_t st)
+cudaError_t launch_joint_step(int g, int k, int sblocks, int vblocks, int rpt, int by, int nsmax,
+                              int mode, cudaStream_t st)
 {
     if constexpr (sizeof(T) == 8) {
-        joint_pair_r<T, 1>(g, it, sblocks, vblocks, by, nsmax, st);
+        joint_pair_r<T, 1>(g, k, sblocks, vblocks, by, nsmax, mode, st);
     } else {
         switch (rpt) {
-        case 2: joint_pair_r<T, 2>(g, it, sblocks, vblocks, by, nsmax, st); break;
-        case 4: joint_pair_r<T, 4>(g, it, sblocks, vblocks, by, nsmax, st); break;
-        default: joint_pair_r<T, 1>(g, it, sblocks, vblocks, by, nsmax, st); break;
+        case 2: joint_pair_r<T, 2>(g, k, sblocks, vblocks, by, nsmax, mode, st); break;
+        case 4: joint_pair_r<T, 4>(g, k, sblocks, vblocks, by, nsmax, mode, st); break;
+        default: joint_pair_r<T, 1>(g, k, sblocks, vblocks, by, nsmax, mode, st); break;
         }
     }
     return cudaGetLastError();
@@ -167,28 +177,38 @@ struct psv_joint {
     long long entry_bytes = 0;
     std::vector<unsigned char> entries;    // host copies of the entries
     cudaStream_t st = nullptr;
-    cudaGraphExec_t graph = nullptr;       // the whole time loop, shape (g_rpt, g_by)
-    int g_rpt = 0, g_by = 0;
+    // whole time loops per velocity mode (forward modelling, gradient
+    // forward, adjoint), each captured with the shape in g_shape
+    cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+    int g_shape[3][2] = {};
     ~psv_joint()
     {
-        if (graph) cudaGraphExecDestroy(graph);
+        for (auto g : graph)
+            if (g) cudaGraphExecDestroy(g);
         if (st) cudaStreamDestroy(st);
     }
 };
 
 namespace {
 
-// Sets every plan to the direct family with rpt rows per thread and 32 x by
-// blocks, zeroes its wavefields, fills the entries, builds the segment
-// tables and launch extents, and uploads both tables.
-int joint_prepare(psv_joint *J, int rpt, int by)
+int mode_slot(int mode) { return mode == psv::MODE_FWD ? 1 : mode == psv::MODE_ADJ ? 2 : 0; }
+
+// Fills every plan's entry: plan k's call fill(k, entry) (joint_begin or a
+// joint gradient phase), its error prefixed with the plan's index.
+template <typename F> int joint_fill(psv_joint *J, F fill)
 {
     const int n = (int)J->plans.size();
     for (int k = 0; k < n; k++) {
-        const int s = J->plans[k]->impl->joint_begin(rpt, by, J->entries.data() + k * J->entry_bytes,
-                                                     (size_t)J->entry_bytes);
+        const int s = fill(k, J->entries.data() + k * J->entry_bytes);
         if (s != PSV_OK) return fail(s, "plan " + std::to_string(k) + ": " + psv_last_error());
     }
+    return PSV_OK;
+}
+
+// Segment tables and launch extents from the filled entries; uploads both.
+int joint_tables(psv_joint *J)
+{
+    const int n = (int)J->plans.size();
     std::vector<int> nt(n);
     std::vector<long long> nsb(n), nvb(n);
     J->nsmax = 1;
@@ -246,20 +266,30 @@ int joint_prepare(psv_joint *J, int rpt, int by)
     return PSV_OK;
 }
 
-// Captures steps [0, nsteps) of the joint loop with shape (rpt, by) into *exec.
-int joint_capture(psv_joint *J, int rpt, int by, int nsteps, cudaGraphExec_t *exec)
+// Forward-modelling entries of every plan with shape (rpt, by), then the tables.
+int joint_prepare(psv_joint *J, int rpt, int by)
+{
+    PSV_TRY(joint_fill(J, [&](int k, void *e) {
+        return J->plans[k]->impl->joint_begin(rpt, by, e, (size_t)J->entry_bytes);
+    }));
+    return joint_tables(J);
+}
+
+// Captures joint steps [0, nsteps) with shape (rpt, by) and velocity mode
+// `mode` into *exec.
+int joint_capture(psv_joint *J, int rpt, int by, int nsteps, int mode, cudaGraphExec_t *exec)
 {
     cudaGraph_t graph = nullptr;
     PSV_CU(cudaStreamBeginCapture(J->st, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    int it = 0;
+    int k = 0;
     for (int g = 0; g < J->nseg && e == cudaSuccess; g++)
-        for (; it < std::min(J->seg_end[g], nsteps) && e == cudaSuccess; it++)
+        for (; k < std::min(J->seg_end[g], nsteps) && e == cudaSuccess; k++)
             e = J->prec == 32
-                    ? psv::launch_joint_step<float>(g, it, (int)J->sblocks[g], (int)J->vblocks[g], rpt, by,
-                                                    J->nsmax, J->st)
-                    : psv::launch_joint_step<double>(g, it, (int)J->sblocks[g], (int)J->vblocks[g], rpt,
-                                                     by, J->nsmax, J->st);
+                    ? psv::launch_joint_step<float>(g, k, (int)J->sblocks[g], (int)J->vblocks[g], rpt, by,
+                                                    J->nsmax, mode, J->st)
+                    : psv::launch_joint_step<double>(g, k, (int)J->sblocks[g], (int)J->vblocks[g], rpt,
+                                                     by, J->nsmax, mode, J->st);
     const cudaError_t ce = cudaStreamEndCapture(J->st, &graph);
     if (e != cudaSuccess || ce != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -292,8 +322,25 @@ int joint_replay(psv_joint *J, cudaGraphExec_t exec, float *ms)
     return PSV_OK;
 }
 
+// The whole joint time loop of velocity mode `mode` (tables uploaded),
+// captured once per shape and replayed.
+int joint_run(psv_joint *J, int mode, float *ms)
+{
+    const int m = mode_slot(mode);
+    if (J->graph[m] && (J->g_shape[m][0] != J->rpt || J->g_shape[m][1] != J->by)) {
+        cudaGraphExecDestroy(J->graph[m]);
+        J->graph[m] = nullptr;
+    }
+    if (!J->graph[m]) {
+        PSV_TRY(joint_capture(J, J->rpt, J->by, J->maxnt, mode, &J->graph[m]));
+        J->g_shape[m][0] = J->rpt;
+        J->g_shape[m][1] = J->by;
+    }
+    return joint_replay(J, J->graph[m], ms);
+}
+
 // Tile shape of the joint launches: each candidate times the first steps of
-// the loop (up to 24, all surveys running), replayed after a warm-up; the
+// the forward-modelling loop (up to 24), replayed after a warm-up; the
 // fastest is kept.  The plans' wavefields are zeroed again by the pass.
 int joint_autotune(psv_joint *J)
 {
@@ -306,7 +353,7 @@ int joint_autotune(psv_joint *J)
         const int r = J->prec == 32 ? f32[c][0] : f64[c][0], b = J->prec == 32 ? f32[c][1] : f64[c][1];
         PSV_TRY(joint_prepare(J, r, b));
         cudaGraphExec_t x = nullptr;
-        PSV_TRY(joint_capture(J, r, b, std::min(24, J->seg_end[0]), &x));
+        PSV_TRY(joint_capture(J, r, b, std::min(24, J->seg_end[0]), psv::MODE_FWD_NOWE, &x));
         float t0 = 0.f, t = 0.f;
         int s = joint_replay(J, x, &t0);
         if (s == PSV_OK) s = joint_replay(J, x, &t);
@@ -370,24 +417,36 @@ int psv_joint_forward(psv_joint *J, double *const *rtf_uz, double *const *rtf_ux
     std::lock_guard<std::mutex> lk(psv::joint_mutex());
     if (J->tune) PSV_TRY(joint_autotune(J));
     PSV_TRY(joint_prepare(J, J->rpt, J->by));
-    if (J->graph && (J->g_rpt != J->rpt || J->g_by != J->by)) {
-        cudaGraphExecDestroy(J->graph);
-        J->graph = nullptr;
-    }
-    if (!J->graph) {
-        PSV_TRY(joint_capture(J, J->rpt, J->by, J->maxnt, &J->graph));
-        J->g_rpt = J->rpt;
-        J->g_by = J->by;
-    }
     float t = 0.f;
-    PSV_TRY(joint_replay(J, J->graph, &t));
+    PSV_TRY(joint_run(J, psv::MODE_FWD_NOWE, &t));
     if (ms) *ms = t;
-    const int n = (int)J->plans.size();
-    for (int k = 0; k < n; k++) {
-        const int s = J->plans[k]->impl->joint_end(rtf_uz ? rtf_uz[k] : nullptr, rtf_ux ? rtf_ux[k] : nullptr);
-        if (s != PSV_OK) return fail(s, "plan " + std::to_string(k) + ": " + psv_last_error());
-    }
-    return PSV_OK;
+    return joint_fill(J, [&](int k, void *) {
+        return J->plans[k]->impl->joint_end(rtf_uz ? rtf_uz[k] : nullptr, rtf_ux ? rtf_ux[k] : nullptr);
+    });
+}
+
+int psv_joint_gradient(psv_joint *J, double *L2, double *ms)
+{
+    if (!J) return fail(PSV_ERR_ARG, "null joint handle");
+    std::lock_guard<std::mutex> lk(psv::joint_mutex());
+    if (J->tune) PSV_TRY(joint_autotune(J));
+    const int r = J->rpt, b = J->by;
+    const size_t eb = (size_t)J->entry_bytes;
+    float tf = 0.f, ta = 0.f;
+    PSV_TRY(joint_fill(J, [&](int k, void *e) {
+        return J->plans[k]->impl->joint_gradient_phase(0, r, b, e, eb, nullptr);
+    }));
+    PSV_TRY(joint_tables(J));
+    PSV_TRY(joint_run(J, psv::MODE_FWD, &tf));
+    PSV_TRY(joint_fill(J, [&](int k, void *e) {
+        return J->plans[k]->impl->joint_gradient_phase(1, r, b, e, eb, nullptr);
+    }));
+    PSV_TRY(joint_tables(J));
+    PSV_TRY(joint_run(J, psv::MODE_ADJ, &ta));
+    if (ms) *ms = tf + ta;
+    return joint_fill(J, [&](int k, void *e) {
+        return J->plans[k]->impl->joint_gradient_phase(2, r, b, e, eb, L2 ? L2 + k : nullptr);
+    });
 }
 
 int psv_joint_shape(const psv_joint *J, int *rows_per_thread, int *block_y)

@@ -112,6 +112,8 @@ struct JointSurvey {
     int ns, nt, nb;  // stencil terms, time steps, shots
     int sx, sy;      // stress grid blocks along x and z
     int vx, vy;      // velocity grid blocks along x and z
+    int rev;         // joint step k is the survey's step nt - 1 - k (adjoint pass), else k
+    int sdt, ring;   // snapshots: every sdt-th step into slot (it / sdt) % ring; sdt 0: none
 };
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
@@ -216,6 +218,12 @@ struct PlanIface {
     // after the joint time loop, fetch the traces.
     virtual int joint_begin(int rpt, int by, void *entry, size_t bytes) = 0;
     virtual int joint_end(double *rtf_uz, double *rtf_ux) = 0;
+    // Joint gradient, the plan's work around the two joint passes: phase 0
+    // sets up the forward pass (as joint_begin, snapshots on), phase 1 forms
+    // the residuals and adjoint sources and sets up the adjoint pass, phase 2
+    // preconditions the shot gradients into the global ones and returns L2.
+    virtual int joint_gradient_phase(int phase, int rpt, int by, void *entry, size_t bytes,
+                                     double *L2) = 0;
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
                             const double *rho_zp, const double *rho_xp, int ishot, int grad,

@@ -1632,9 +1632,16 @@ public:
         PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
         PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+        joint_entry(entry, r, by, qf, false, false);
+        PSV_CU(cudaStreamSynchronize(st));
+        return PSV_OK;
+    }
+
+    void joint_entry(void *entry, int r, int by, const SrcRecParams<T> &q, bool rev, bool snaps) const
+    {
         JointSurvey<T> &e = *static_cast<JointSurvey<T> *>(entry);
         e.p = sp;
-        e.q = qf;
+        e.q = q;
         e.ns = sv.ns;
         e.nt = sv.g.nt;
         e.nb = B;
@@ -1643,6 +1650,66 @@ public:
         e.sy = (sv.nz2 - sv.nz1 + tz - 1) / tz;
         e.vx = (sv.g.nx + 31) / 32;
         e.vy = (sv.g.nz + tz - 1) / tz;
+        e.rev = rev ? 1 : 0;
+        e.sdt = snaps ? sv.g.snap_dt : 0;
+        e.ring = sv.snt;
+    }
+
+    int joint_gradient_phase(int phase, int r, int by, void *entry, size_t bytes, double *L2) override
+    {
+        T *f = fld.as<T>();
+        if (phase == 0) {
+            if (bytes != sizeof(JointSurvey<T>))
+                return fail(PSV_ERR_ARG, "joint launch: every plan of one precision");
+            if (!have_model || !have_obs)
+                return fail(PSV_ERR_ARG, "joint gradient: a plan without model or observed traces");
+            if (opt.adjoint == PSV_ADJOINT_EXACT)
+                return fail(PSV_ERR_UNSUPPORTED, "joint gradient: the reference-mode adjoint only");
+            if (nbatch != 1)
+                return fail(PSV_ERR_UNSUPPORTED, "joint launch: every shot of a survey in one batch "
+                                                 "(max_batch >= nshot)");
+            if (ckpt)
+                return fail(PSV_ERR_UNSUPPORTED, "joint gradient: full snapshot storage only "
+                                                 "(storage = full)");
+            PSV_TRY(ensure_hist());
+            PSV_TRY(coefficients(true, false));
+            PSV_TRY(set_shape(PSV_KERNELS_DIRECT, r, by));
+            if (fam != PSV_KERNELS_DIRECT || rpt != r || (int)blk.y != by)
+                return fail(PSV_ERR_ARG, "joint launch: unsupported tile shape");
+            PSV_TRY(set_batch(0));
+            last_batch_s0 = 0;
+            // the gradient forward pass's resets (enqueue, MODE_FWD)
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WE * plane, plane, B, st));
+            PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+            PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+            joint_entry(entry, r, by, qf, false, true);
+        } else if (phase == 1) {
+            // residuals, L2 and adjoint sources (as gradient()), then the
+            // adjoint pass's resets (enqueue, MODE_ADJ)
+            PSV_CU(launch_adjsrc(tr(0), tr(1), tr(2), tr(3), tr(4), tr(5), ntr, B, sv.g.dt, partial(),
+                                 L2dev(), st));
+            PSV_CU(launch_adjoint_scale(tr(4), tr(5), ntr, B, inj, rmax(), ascale(), st));
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 7 * plane, B, st));
+            PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WEA * plane, plane, B, st));
+            PSV_CU(launch_zero_planes<T>(gshot.as<T>(), gshot_shot, 0, gshot_shot, B, st));
+            PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
+            PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
+            joint_entry(entry, r, by, qa, true, true);
+        } else {
+            if (opt.smooth_hfs >= 2) PSV_TRY(smooth_shot_gradients(B));
+            PSV_TRY(precondition(B));
+            PSV_TRY(sync_check());
+            last_s0 = 0;
+            last_n = B;
+            const int nshot = sv.s.nshot;
+            L2_shot.assign(nshot, 0.0);
+            PSV_CU(cudaMemcpy(L2_shot.data(), L2dev(), nshot * 8, cudaMemcpyDeviceToHost));
+            double s = 0.0;
+            for (int i = 0; i < nshot; i++) s += L2_shot[i];
+            if (L2) *L2 = s;
+            return PSV_OK;
+        }
         PSV_CU(cudaStreamSynchronize(st));
         return PSV_OK;
     }

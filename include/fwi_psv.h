@@ -242,7 +242,7 @@ int psv_multi_forward(psv_plan *const *plans, int nplans, double *const *rtf_uz,
                       double *const *rtf_ux);
 int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
 
-/* Joint forward modelling: up to 8 surveys (one plan each, all of one
+/* Joint passes: up to 8 surveys (one plan each, all of one
  * precision, every shot of a plan in one batch: max_batch >= nshot) stepped
  * in ONE stress launch and ONE velocity launch per time step, whose blocks
  * cover every shot of every survey still running.  Grid sizes, stencil
@@ -266,8 +266,19 @@ int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
  *     agree to rounding (FP32 relative L2 ~1e-8), not bit for bit.  One
  *     joint pass runs at a time per process (the survey tables are in
  *     constant memory).
- *   psv_joint_launches: kernel launches of one psv_joint_forward (2 x the
- *     longest step count; 0 before the first call).
+ *   psv_joint_gradient: psv_gradient of every plan, each holding its full
+ *     snapshot history (PSV_STORE_FULL, or AUTO resolving to it) and its
+ *     observed traces: the gradient forward pass of all surveys in one
+ *     launch pair per step, residuals and adjoint sources per plan, the
+ *     adjoint pass of all surveys in one launch pair per step (each survey
+ *     at its own time-reversed step), preconditioning per plan.  L2[k] per
+ *     plan (may be NULL); the global gradients stay on each plan
+ *     (psv_get_gradient); *ms (may be NULL) the device time of the two
+ *     joint passes.  Gradients agree with each plan's own psv_gradient with
+ *     the same tile shape to rounding.  PSV_ERR_UNSUPPORTED for checkpointed
+ *     storage or the exact adjoint.
+ *   psv_joint_launches: kernel launches of one joint pass (2 x the longest
+ *     step count; 0 before the first call).
  * Errors: PSV_ERR_ARG (more than 8 plans, mixed precisions, a plan twice,
  * no model), PSV_ERR_UNSUPPORTED (a plan with more than one batch).  No
  * counterpart in the reference (one survey per program run). */
@@ -275,6 +286,7 @@ typedef struct psv_joint psv_joint;
 int psv_joint_create(psv_plan *const *plans, int nplans, int rows_per_thread, int block_y,
                      psv_joint **out);
 int psv_joint_forward(psv_joint *joint, double *const *rtf_uz, double *const *rtf_ux, double *ms);
+int psv_joint_gradient(psv_joint *joint, double *L2, double *ms);
 long long psv_joint_launches(const psv_joint *joint);
 int psv_joint_shape(const psv_joint *joint, int *rows_per_thread, int *block_y);
 int psv_joint_destroy(psv_joint *joint);
