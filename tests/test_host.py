@@ -286,6 +286,13 @@ def test_compute_calls_refuse_null_arguments():
     assert L.psv_multi_forward(None, 0, None, None) == _lib.PSV_ERR_ARG
     assert L.psv_multi_gradient(None, 0, None) == _lib.PSV_ERR_ARG
     assert L.psv_multi_forward((C.c_void_p * 2)(None, None), 2, None, None) == _lib.PSV_ERR_ARG
+    out = C.c_void_p()
+    assert L.psv_joint_create(None, 0, 1, 4, C.byref(out)) == _lib.PSV_ERR_ARG
+    assert L.psv_joint_create((C.c_void_p * 9)(), 9, 1, 4, C.byref(out)) == _lib.PSV_ERR_ARG
+    assert b"1 to 8" in L.psv_last_error()
+    assert L.psv_joint_create((C.c_void_p * 2)(None, None), 2, 1, 4, C.byref(out)) == _lib.PSV_ERR_ARG
+    assert L.psv_joint_create((C.c_void_p * 1)(None), 1, 1, 4, None) == _lib.PSV_ERR_ARG
+    assert not out
     assert L.psv_misfit(None, None, None, None, None, None, 1, 1, 1, 1.0, None) == _lib.PSV_ERR_ARG
     assert L.psv_misfit_noalloc(None, None, None, None, None, None, 1, 1, 1, 1.0, None,
                                 None) == _lib.PSV_ERR_ARG
