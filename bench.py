@@ -760,6 +760,59 @@ FULL = {  # the batched-survey and the large single-model configurations
 }
 
 
+UNEVEN_FULL_NT = (4000, 6000, 8000, 12000)
+
+
+def run_uneven_full(args):
+    """The uneven batch at its stated shape (--config c4): the four surveys
+    of the uneven-batch leg (401x801 to 1501x3001, 32 shots each, orders 4
+    and 8 mixed, CPML 20-40, Ricker peaks 60-120 Hz) with their full time
+    axes (4000, 6000, 8000, 12000 steps; --crop-nt M caps each), 45 GB of
+    device memory per plan (checkpointed storage where the history does not
+    fit).  Observed data from the true models, then one FWI gradient of all
+    four through psv_multi_gradient (concurrent).  Prints one JSON line:
+    wall seconds, forward + adjoint updates/s over the four surveys (the
+    recomputed forwards not counted), each plan's storage, kernels and
+    device time."""
+    from fwi_cuda_gb300 import engine, survey as S
+    plans, pts = [], 0.0
+    nts = [min(n, args.crop_nt) if args.crop_nt else n for n in UNEVEN_FULL_NT]
+    try:
+        t0 = time.perf_counter()
+        for k, ((nz, nx, _, fd, npml, fc), nt) in enumerate(zip(UNEVEN, nts)):
+            sv, true, init = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=UNEVEN_SHOTS,
+                                              fdorder=fd, npml=npml, nrec=200, snap_dt=3,
+                                              fc=fc, seed=100 + k, surf_offset=0)
+            sv.imaging_sign = 1
+            p = engine.Plan(sv, precision=32, hbm_budget_gb=45.0, **plan_kernels(args))
+            plans.append(p)
+            p.set_model(*true)
+            obs = p.forward()
+            p.set_model(*init)
+            p.set_observed(*obs)
+            pts += 2.0 * UNEVEN_SHOTS * nt * nz * nx
+        t_obs = time.perf_counter() - t0
+        for p in plans:  # tune serially, as psv_multi_gradient does
+            p.autotune()
+        t1 = time.perf_counter()
+        L2 = engine.multi_gradient(plans)
+        sec = time.perf_counter() - t1
+        per = []
+        for p, (nz, nx, *_), nt in zip(plans, UNEVEN, nts):
+            kind, seg, slots, _ = p.storage
+            per.append({"grid": f"{nz}x{nx}", "nt": nt, "storage": kind, "segment_steps": seg,
+                        "slots_per_shot": slots, "device_gb": p.device_bytes / 1e9,
+                        "kernels": dict(zip(("family", "rows_per_thread", "block_y"), p.shape)),
+                        "device_ms": p.timing()})
+        print(json.dumps({"config": "c4", "cropped_nt": bool(args.crop_nt), "nt": nts,
+                          "shots": 4 * UNEVEN_SHOTS, "gradient_s": sec,
+                          "updates_per_s": pts / sec, "observed_data_s": t_obs,
+                          "L2": [float(x) for x in L2], "surveys": per}), flush=True)
+    finally:
+        for p in plans:
+            p.close()
+
+
 def run_full_config(args):
     """One FWI gradient of a full configuration (--config c3 | c5): seeded
     dipping layered model (vp in [1500, 4500] m/s, Gardner rho, vs = vp/1.73,
@@ -884,7 +937,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--grid", choices=["bench", "large"], default="bench",
                     help="--profile workload: the 301x601 bench grid or the 1001x2001 grid")
-    ap.add_argument("--config", choices=["c3", "c5"], default=None,
+    ap.add_argument("--config", choices=["c3", "c4", "c5"], default=None,
                     help="run one gradient of a full configuration instead of the bench")
     ap.add_argument("--storage", choices=["checkpoint", "binomial"], default="checkpoint",
                     help="snapshot storage of the --config runs")
@@ -917,6 +970,8 @@ def main():
     ap.add_argument("--nt", type=int, default=400, help="time steps of the --profile case")
     ap.add_argument("--nshot", type=int, default=2, help="shots of the --profile case")
     args = ap.parse_args()
+    if args.config == "c4":
+        return run_uneven_full(args)
     if args.config:
         return run_full_config(args)
     if args.profile:
