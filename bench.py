@@ -770,10 +770,12 @@ def run_uneven_full(args):
     axes (4000, 6000, 8000, 12000 steps; --crop-nt M caps each), 45 GB of
     device memory per plan (checkpointed storage where the history does not
     fit).  Observed data from the true models, then one FWI gradient of all
-    four through psv_multi_gradient (concurrent).  Prints one JSON line:
-    wall seconds, forward + adjoint updates/s over the four surveys (the
-    recomputed forwards not counted), each plan's storage, kernels and
-    device time."""
+    four through psv_multi_gradient (concurrent), or with --joint through
+    psv_joint_gradient (one stress and one velocity launch per joint step
+    over batch b of all four surveys, the direct family).
+    Prints one JSON line: wall seconds, forward + adjoint updates/s over the
+    four surveys (the recomputed forwards not counted), each plan's storage,
+    kernels and device time (concurrent), or the joint shape and launches."""
     from fwi_cuda_gb300 import engine, survey as S
     plans, pts = [], 0.0
     nts = [min(n, args.crop_nt) if args.crop_nt else n for n in UNEVEN_FULL_NT]
@@ -792,6 +794,21 @@ def run_uneven_full(args):
             p.set_observed(*obs)
             pts += 2.0 * UNEVEN_SHOTS * nt * nz * nx
         t_obs = time.perf_counter() - t0
+        if args.joint:
+            with engine.Joint(plans) as J:
+                t1 = time.perf_counter()
+                L2 = J.gradient()
+                sec = time.perf_counter() - t1
+                shape, nl, dev = J.shape, J.launches(), J.ms
+            print(json.dumps({"config": "c4", "joint": True, "cropped_nt": bool(args.crop_nt), "nt": nts,
+                              "shots": 4 * UNEVEN_SHOTS, "gradient_s": sec,
+                              "gradient_s_includes": "the joint shape autotune and graph captures",
+                              "updates_per_s": pts / sec, "device_s": dev * 1e-3,
+                              "device_updates_per_s": pts / (dev * 1e-3), "observed_data_s": t_obs,
+                              "joint_shape": shape, "launches": nl,
+                              "storage": [p.storage[0] for p in plans],
+                              "L2": [float(x) for x in L2]}), flush=True)
+            return
         for p in plans:  # tune serially, as psv_multi_gradient does
             p.autotune()
         t1 = time.perf_counter()
@@ -949,6 +966,8 @@ def main():
                     help="with --config: run the first N time steps only")
     ap.add_argument("--slots", type=int, default=0,
                     help="state slots per shot with --storage binomial (0 = the library's choice)")
+    ap.add_argument("--joint", action="store_true",
+                    help="--config c4: the gradient through the joint launches")
     ap.add_argument("--no-uneven", action="store_true",
                     help="skip the multi-survey legs (uneven grids, small surveys)")
     ap.add_argument("--no-large", action="store_true",

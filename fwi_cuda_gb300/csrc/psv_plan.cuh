@@ -107,13 +107,27 @@ cudaError_t launch_exact_chain(const StepParams<double> &p, const ExactBufs &X, 
 constexpr int JOINT_MAX = 8;
 template <typename T>
 struct JointSurvey {
-    StepParams<T> p;
-    SrcRecParams<T> q;
-    int ns, nt, nb;  // stencil terms, time steps, shots
-    int sx, sy;      // stress grid blocks along x and z
-    int vx, vy;      // velocity grid blocks along x and z
-    int rev;         // joint step k is the survey's step nt - 1 - k (adjoint pass), else k
-    int sdt, ring;   // snapshots: every sdt-th step into slot (it / sdt) % ring; sdt 0: none
+    StepParams<T> p, p2;   // the main state and the checkpoint recompute state
+    SrcRecParams<T> q[3];  // sources / receivers: forward, recompute, adjoint
+    const int4 *ops;       // the pass's step descriptors (device), one per joint step
+    int nops;              // steps of the survey in the pass
+    int ns, nb;            // stencil terms, shots
+    int sx, sy;            // stress grid blocks along x and z
+    int vx, vy;            // velocity grid blocks along x and z
+};
+// Step descriptor: x = state | source set << 1 | velocity mode << 3 (state 0
+// main, 1 recompute; set 0 forward, 1 recompute, 2 adjoint), y = the
+// survey's own time step, z = snapshot slot or -1.
+__host__ __device__ constexpr int joint_flags(int state, int qsel, int mode)
+{
+    return state | qsel << 1 | mode << 3;
+}
+// One operation of a survey's joint pass: a time step (its descriptor), or a
+// checkpoint copy (slot, operation, field copy) before the survey's next step.
+struct JointOp {
+    int copy;
+    int flags, it, slot;
+    int ck_slot, ck_op, par;
 };
 cudaError_t launch_stress_tma(const StepParams<float> &p, const TileMaps &m, int ns, int rpt,
                               int nbatch, cudaStream_t st);
@@ -213,17 +227,24 @@ struct PlanIface {
     virtual int chain_count() const = 0;
     virtual int prepare() = 0;  // history buffers and the pending autotune, before concurrent use
     // Joint forward modelling (psv_joint.cu): switch to the direct family with
-    // rpt rows per thread and 32 x by blocks, zero the wavefields, fill the
-    // JointSurvey<T> at `entry` (`bytes` = its size: the precisions agree);
-    // after the joint time loop, fetch the traces.
-    virtual int joint_begin(int rpt, int by, void *entry, size_t bytes) = 0;
+    // rpt rows per thread and 32 x by blocks, select shot batch `batch`, zero
+    // the wavefields, fill the JointSurvey<T> at `entry` (`bytes` = its size:
+    // the precisions agree) and the pass's operations; after the joint time
+    // loops of every batch, fetch the traces.
+    virtual int joint_begin(int rpt, int by, int batch, void *entry, size_t bytes,
+                            std::vector<JointOp> *ops) = 0;
     virtual int joint_end(double *rtf_uz, double *rtf_ux) = 0;
+    virtual int batches() const = 0;  // shot batches of the plan (max_batch, HBM budget)
     // Joint gradient, the plan's work around the two joint passes: phase 0
-    // sets up the forward pass (as joint_begin, snapshots on), phase 1 forms
-    // the residuals and adjoint sources and sets up the adjoint pass, phase 2
-    // preconditions the shot gradients into the global ones and returns L2.
-    virtual int joint_gradient_phase(int phase, int rpt, int by, void *entry, size_t bytes,
-                                     double *L2) = 0;
+    // sets up the forward pass (as joint_begin; snapshots, or checkpoint
+    // saves), phase 1 forms the residuals and adjoint sources and sets up the
+    // adjoint pass (with checkpoints: the schedule's restores, recomputed
+    // segments and adjoint steps), phase 2 preconditions the shot gradients
+    // into the global ones and returns L2.
+    virtual int joint_gradient_phase(int phase, int rpt, int by, int batch, void *entry,
+                                     size_t bytes, double *L2, std::vector<JointOp> *ops) = 0;
+    // A checkpoint copy of the plan's schedule, enqueued on `stream`.
+    virtual int joint_ck_copy(int slot, int op, int par, void *stream) = 0;
     // kernel_PSV drop-in support
     virtual int kernel_call(const double *lam, const double *mu, const double *mu_zx,
                             const double *rho_zp, const double *rho_xp, int ishot, int grad,

@@ -794,8 +794,9 @@ public:
     // state (CK_SAVE_MAIN) or the working state (CK_SAVE_WORK, CK_RESTORE),
     // taking v and sigma from / to copy pr.  The CPML strips are copied
     // whole (both copies of the ping-ponged memories).
-    int ck_copy(int j, int op, int pr)
+    int ck_copy(int j, int op, int pr, cudaStream_t cs = nullptr)
     {
+        const cudaStream_t st = cs ? cs : this->st;
         T *c = ck.as<T>() + (size_t)j * B * ck_state;
         const size_t cp = (size_t)ck_state * sizeof(T);
         const bool main = op == CK_SAVE_MAIN, save = op != CK_RESTORE;
@@ -1615,49 +1616,115 @@ public:
         return maybe_autotune();
     }
 
-    int joint_begin(int r, int by, void *entry, size_t bytes) override
+    int batches() const override { return nbatch; }
+
+    int joint_begin(int r, int by, int batch, void *entry, size_t bytes,
+                    std::vector<JointOp> *ops) override
     {
         if (bytes != sizeof(JointSurvey<T>))
             return fail(PSV_ERR_ARG, "joint launch: every plan of one precision");
         if (!have_model) return fail(PSV_ERR_ARG, "joint launch: a plan has no model");
-        if (nbatch != 1)
-            return fail(PSV_ERR_UNSUPPORTED, "joint launch: every shot of a survey in one batch "
-                                             "(max_batch >= nshot)");
+        if (batch < 0 || batch >= nbatch) return fail(PSV_ERR_ARG, "joint launch: no such shot batch");
         PSV_TRY(set_shape(PSV_KERNELS_DIRECT, r, by));
         if (fam != PSV_KERNELS_DIRECT || rpt != r || (int)blk.y != by)
             return fail(PSV_ERR_ARG, "joint launch: unsupported tile shape");
-        PSV_TRY(set_batch(0));
+        PSV_TRY(set_batch(batch));
         // reset_sv2 / reset_PML_memory2 (n_kernel_PSV.cpp:74-88), as the plain forward pass
         T *f = fld.as<T>();
         PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
         PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
         PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
-        joint_entry(entry, r, by, qf, false, false);
+        joint_entry(entry, r, by);
+        ops->clear();
+        for (int it = 0; it < sv.g.nt; it++) ops->push_back(joint_step(0, 0, MODE_FWD_NOWE, it, -1));
         PSV_CU(cudaStreamSynchronize(st));
         return PSV_OK;
     }
 
-    void joint_entry(void *entry, int r, int by, const SrcRecParams<T> &q, bool rev, bool snaps) const
+    int joint_end(double *uz, double *ux) override
+    {
+        if (uz && sv.s.nrec) PSV_TRY(download_traces(uz, tr(0), 0, sv.s.nshot));
+        if (ux && sv.s.nrec) PSV_TRY(download_traces(ux, tr(1), 0, sv.s.nshot));
+        return sync_check();
+    }
+
+    static JointOp joint_step(int state, int qsel, int mode, int it, int slot)
+    {
+        return JointOp{0, joint_flags(state, qsel, mode), it, slot, 0, 0, 0};
+    }
+
+    void joint_entry(void *entry, int r, int by) const
     {
         JointSurvey<T> &e = *static_cast<JointSurvey<T> *>(entry);
         e.p = sp;
-        e.q = q;
+        e.p2 = sp2;
+        e.q[0] = qf;
+        e.q[1] = qr;
+        e.q[2] = qa;
+        e.ops = nullptr;
+        e.nops = 0;
         e.ns = sv.ns;
-        e.nt = sv.g.nt;
         e.nb = B;
         const int tz = by * r;
         e.sx = (sv.nx2 - sv.nx1 + 31) / 32;
         e.sy = (sv.nz2 - sv.nz1 + tz - 1) / tz;
         e.vx = (sv.g.nx + 31) / 32;
         e.vy = (sv.g.nz + tz - 1) / tz;
-        e.rev = rev ? 1 : 0;
-        e.sdt = snaps ? sv.g.snap_dt : 0;
-        e.ring = sv.snt;
     }
 
-    int joint_gradient_phase(int phase, int r, int by, void *entry, size_t bytes, double *L2) override
+    int joint_ck_copy(int slot, int op, int par, void *stream) override
+    {
+        return ck_copy(slot, op, par, (cudaStream_t)stream);
+    }
+
+    // The operations of the gradient's forward pass (enqueue, PASS_FWD_STORE):
+    // steps with snapshots, or with checkpoint saves at segment starts.
+    void joint_forward_ops(std::vector<JointOp> *ops) const
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        ops->clear();
+        for (int it = 0; it < nt; it++) {
+            if (ckpt && !(it % K) && fwd_slot[(size_t)(it / K)] >= 0)
+                ops->push_back(JointOp{1, 0, 0, 0, fwd_slot[(size_t)(it / K)], CK_SAVE_MAIN, par(it)});
+            const int slot = !ckpt && !(it % sdt) ? it / sdt : -1;
+            ops->push_back(joint_step(0, 0, MODE_FWD, it, slot));
+        }
+    }
+
+    // The operations of the adjoint pass (enqueue, PASS_ADJ_RES): reversed
+    // steps with imaging, or the checkpoint schedule (run_schedule).
+    void joint_adjoint_ops(std::vector<JointOp> *ops) const
+    {
+        const int nt = sv.g.nt, sdt = sv.g.snap_dt;
+        ops->clear();
+        if (!ckpt) {
+            for (int jt = 0; jt < nt; jt++) {
+                const int it = nt - 1 - jt;
+                ops->push_back(joint_step(0, 2, MODE_ADJ, it, !(it % sdt) ? it / sdt : -1));
+            }
+            return;
+        }
+        for (const CkAction &x : sched.bwd) {
+            const int a = x.seg * K, e = std::min(a + K, nt);
+            if (x.op == CK_RESTORE || x.op == CK_SAVE_WORK) {
+                ops->push_back(JointOp{1, 0, 0, 0, x.slot, x.op, par(a)});
+            } else if (x.op == CK_ADVANCE) {
+                for (int it = a; it < e; it++) ops->push_back(joint_step(1, 1, MODE_FWD_NOWE, it, -1));
+            } else if (x.op == CK_REVERSE) {
+                const int base = (a + sdt - 1) / sdt, last = (e - 1) / sdt * sdt;
+                for (int it = a; it <= last; it++)
+                    ops->push_back(joint_step(1, 1, MODE_FWD_NOWE, it, !(it % sdt) ? it / sdt - base : -1));
+                for (int it = e - 1; it >= a; it--)
+                    ops->push_back(joint_step(0, 2, MODE_ADJ, it, !(it % sdt) ? it / sdt - base : -1));
+            }
+        }
+    }
+
+    int joint_gradient_phase(int phase, int r, int by, int batch, void *entry, size_t bytes,
+                             double *L2, std::vector<JointOp> *ops) override
     {
         T *f = fld.as<T>();
+        const int s0 = batch * B, n = std::min(B, sv.s.nshot - s0);
         if (phase == 0) {
             if (bytes != sizeof(JointSurvey<T>))
                 return fail(PSV_ERR_ARG, "joint launch: every plan of one precision");
@@ -1665,43 +1732,45 @@ public:
                 return fail(PSV_ERR_ARG, "joint gradient: a plan without model or observed traces");
             if (opt.adjoint == PSV_ADJOINT_EXACT)
                 return fail(PSV_ERR_UNSUPPORTED, "joint gradient: the reference-mode adjoint only");
-            if (nbatch != 1)
-                return fail(PSV_ERR_UNSUPPORTED, "joint launch: every shot of a survey in one batch "
-                                                 "(max_batch >= nshot)");
-            if (ckpt)
-                return fail(PSV_ERR_UNSUPPORTED, "joint gradient: full snapshot storage only "
-                                                 "(storage = full)");
-            PSV_TRY(ensure_hist());
-            PSV_TRY(coefficients(true, false));
+            if (batch < 0 || batch >= nbatch) return fail(PSV_ERR_ARG, "joint launch: no such shot batch");
+            if (batch == 0) {
+                PSV_TRY(ensure_hist());
+                PSV_TRY(coefficients(true, false));
+            }
             PSV_TRY(set_shape(PSV_KERNELS_DIRECT, r, by));
             if (fam != PSV_KERNELS_DIRECT || rpt != r || (int)blk.y != by)
                 return fail(PSV_ERR_ARG, "joint launch: unsupported tile shape");
-            PSV_TRY(set_batch(0));
-            last_batch_s0 = 0;
+            PSV_TRY(set_batch(batch));
+            last_batch_s0 = s0;
             // the gradient forward pass's resets (enqueue, MODE_FWD)
             PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 5 * plane, B, st));
             PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WE * plane, plane, B, st));
             PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
             PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
-            joint_entry(entry, r, by, qf, false, true);
+            joint_entry(entry, r, by);
+            joint_forward_ops(ops);
         } else if (phase == 1) {
             // residuals, L2 and adjoint sources (as gradient()), then the
             // adjoint pass's resets (enqueue, MODE_ADJ)
-            PSV_CU(launch_adjsrc(tr(0), tr(1), tr(2), tr(3), tr(4), tr(5), ntr, B, sv.g.dt, partial(),
-                                 L2dev(), st));
-            PSV_CU(launch_adjoint_scale(tr(4), tr(5), ntr, B, inj, rmax(), ascale(), st));
+            PSV_CU(launch_adjsrc(tr(0) + s0 * ntr, tr(1) + s0 * ntr, tr(2) + s0 * ntr,
+                                 tr(3) + s0 * ntr, tr(4) + s0 * ntr, tr(5) + s0 * ntr, ntr, n,
+                                 sv.g.dt, partial(), L2dev() + s0, st));
+            PSV_CU(launch_adjoint_scale(tr(4) + s0 * ntr, tr(5) + s0 * ntr, ntr, n, inj,
+                                        rmax() + s0, ascale() + s0, st));
             PSV_CU(launch_zero_planes<T>(f, shot_stride, 0, 7 * plane, B, st));
             PSV_CU(launch_zero_planes<T>(f, shot_stride, F_WEA * plane, plane, B, st));
             PSV_CU(launch_zero_planes<T>(gshot.as<T>(), gshot_shot, 0, gshot_shot, B, st));
             PSV_CU(launch_zero_planes<T>(memz.as<T>(), mz_shot, 0, mz_shot, B, st));
             PSV_CU(launch_zero_planes<T>(memx.as<T>(), mx_shot, 0, mx_shot, B, st));
-            joint_entry(entry, r, by, qa, true, true);
+            joint_entry(entry, r, by);
+            joint_adjoint_ops(ops);
         } else {
-            if (opt.smooth_hfs >= 2) PSV_TRY(smooth_shot_gradients(B));
-            PSV_TRY(precondition(B));
+            if (opt.smooth_hfs >= 2) PSV_TRY(smooth_shot_gradients(n));
+            PSV_TRY(precondition(n));
             PSV_TRY(sync_check());
-            last_s0 = 0;
-            last_n = B;
+            last_s0 = s0;
+            last_n = n;
+            if (batch + 1 < nbatch) return PSV_OK;  // L2 after the last batch
             const int nshot = sv.s.nshot;
             L2_shot.assign(nshot, 0.0);
             PSV_CU(cudaMemcpy(L2_shot.data(), L2dev(), nshot * 8, cudaMemcpyDeviceToHost));
@@ -1712,13 +1781,6 @@ public:
         }
         PSV_CU(cudaStreamSynchronize(st));
         return PSV_OK;
-    }
-
-    int joint_end(double *uz, double *ux) override
-    {
-        if (uz && sv.s.nrec) PSV_TRY(download_traces(uz, tr(0), 0, sv.s.nshot));
-        if (ux && sv.s.nrec) PSV_TRY(download_traces(ux, tr(1), 0, sv.s.nshot));
-        return sync_check();
     }
 
     int maybe_autotune()

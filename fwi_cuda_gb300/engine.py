@@ -342,7 +342,7 @@ def multi_forward(plans):
 
 class Joint:
     """psv_joint_*: forward modelling or FWI gradients of up to 8 surveys
-    (one Plan each, one precision, every shot in one batch) in one stress and
+    (one Plan each, one precision; batch b of every plan at once) in one stress and
     one velocity launch per time step; grid sizes, stencil orders, shot and
     step counts may differ.  The plans run the direct kernel family with the joint tile
     shape (rows_per_thread x 32 x block_y threads; rows_per_thread 0: chosen
@@ -374,9 +374,9 @@ class Joint:
         return out
 
     def gradient(self):
-        """One FWI gradient of every survey (full snapshot storage) through
-        the two joint passes; returns L2 per plan, the gradients stay on the
-        plans.  self.ms holds the device time of the two passes."""
+        """One FWI gradient of every survey (any storage) through the two
+        joint passes of each shot batch; returns L2 per plan, the gradients
+        stay on the plans.  self.ms holds the device time of the passes."""
         L2 = np.zeros(len(self.plans))
         ms = np.zeros(1)
         check(_lib.lib().psv_joint_gradient(self.h, dptr(L2), dptr(ms)))

@@ -242,16 +242,17 @@ int psv_multi_forward(psv_plan *const *plans, int nplans, double *const *rtf_uz,
                       double *const *rtf_ux);
 int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
 
-/* Joint passes: up to 8 surveys (one plan each, all of one
- * precision, every shot of a plan in one batch: max_batch >= nshot) stepped
- * in ONE stress launch and ONE velocity launch per time step, whose blocks
- * cover every shot of every survey still running.  Grid sizes, stencil
- * orders (mixed in one launch), shot counts and step counts may differ; a
- * survey leaves the launches after its last step.  The time loop is one
- * CUDA graph, captured by the first psv_joint_forward and replayed by the
- * later ones.
+/* Joint passes: up to 8 surveys (one plan each, all of one precision)
+ * stepped in ONE stress launch and ONE velocity launch per time step, whose
+ * blocks cover every shot of every survey still running.  Grid sizes,
+ * stencil orders (mixed in one launch), shot counts and step counts may
+ * differ; a survey leaves the launches after its last step.  Plans whose
+ * shots take several batches (max_batch, HBM budget) run batch by batch:
+ * the joint launches cover batch b of every plan that has one.  Each pass
+ * of each batch is one CUDA graph, captured by the first call and replayed
+ * by the later ones.
  *   psv_joint_create: the plans and the tile shape of the joint launches
- *     (rows_per_thread 1, 2 or 4, FP64: 1; blocks of 32 x block_y threads,
+ *     (rows_per_thread 1 or 2, FP64: 1; blocks of 32 x block_y threads,
  *     block_y 1..8), or rows_per_thread 0: the first psv_joint_forward
  *     times the first steps (up to 24) of the joint loop for each of a few
  *     shapes and keeps the fastest.  Every psv_joint_forward sets each plan
@@ -266,22 +267,24 @@ int psv_multi_gradient(psv_plan *const *plans, int nplans, double *L2);
  *     agree to rounding (FP32 relative L2 ~1e-8), not bit for bit.  One
  *     joint pass runs at a time per process (the survey tables are in
  *     constant memory).
- *   psv_joint_gradient: psv_gradient of every plan, each holding its full
- *     snapshot history (PSV_STORE_FULL, or AUTO resolving to it) and its
- *     observed traces: the gradient forward pass of all surveys in one
- *     launch pair per step, residuals and adjoint sources per plan, the
- *     adjoint pass of all surveys in one launch pair per step (each survey
- *     at its own time-reversed step), preconditioning per plan.  L2[k] per
- *     plan (may be NULL); the global gradients stay on each plan
- *     (psv_get_gradient); *ms (may be NULL) the device time of the two
- *     joint passes.  Gradients agree with each plan's own psv_gradient with
- *     the same tile shape to rounding.  PSV_ERR_UNSUPPORTED for checkpointed
- *     storage or the exact adjoint.
- *   psv_joint_launches: kernel launches of one joint pass (2 x the longest
- *     step count; 0 before the first call).
+ *   psv_joint_gradient: psv_gradient of every plan (with its observed
+ *     traces; any storage: full history, two-level or binomial
+ *     checkpoints): the gradient forward pass of all surveys in one launch
+ *     pair per joint step, residuals and adjoint sources per plan, then the
+ *     adjoint pass of all surveys in one launch pair per joint step, each
+ *     survey at its own step of its own sequence (time-reversed adjoint
+ *     steps, and with checkpoints its schedule's recomputed segments, the
+ *     state copies enqueued between the launches), preconditioning per
+ *     plan.  L2[k] per plan (may be NULL); the global gradients stay on
+ *     each plan (psv_get_gradient); *ms (may be NULL) the device time of
+ *     the two joint passes.  Gradients agree with each plan's own
+ *     psv_gradient with the same tile shape to rounding.
+ *     PSV_ERR_UNSUPPORTED for the exact adjoint.
+ *   psv_joint_launches: kernel launches of the last psv_joint_forward or
+ *     psv_joint_gradient (two per joint step; 0 before the first call).
  * Errors: PSV_ERR_ARG (more than 8 plans, mixed precisions, a plan twice,
- * no model), PSV_ERR_UNSUPPORTED (a plan with more than one batch).  No
- * counterpart in the reference (one survey per program run). */
+ * no model or no observed traces).  No counterpart in the reference (one
+ * survey per program run). */
 typedef struct psv_joint psv_joint;
 int psv_joint_create(psv_plan *const *plans, int nplans, int rows_per_thread, int block_y,
                      psv_joint **out);
