@@ -87,3 +87,32 @@ def test_step_byte_model():
     assert t["forward"] == 8.0 + 20.0 / 3 and t["adjoint"] == 44.0 / 3
     assert b.read_traffic("k_velocity_tma_adj", "dram_traffic_large.txt") == 1062.8e6
     assert b.read_traffic("k_stress_tma_fwd", "dram_traffic_large.txt") == 528.6e6
+
+
+def test_uneven_batch_configuration():
+    # the uneven batch at its stated shape (bench.py --config c4): four
+    # seeded layered surveys 401x801, 601x1201, 1001x2001, 1501x3001 with
+    # nt 4000, 6000, 8000, 12000, 32 shots each (128), orders 4 and 8 mixed,
+    # 20-40-cell CPML, Ricker peaks in [60, 120] Hz; each time step below
+    # its survey's stability limit (checkfd_ssg_elastic)
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    from fwi_cuda_gb300 import _lib, survey as S
+    from fwi_cuda_gb300._lib import dptr
+    assert bench.UNEVEN_SHOTS == 32 and bench.UNEVEN_FULL_NT == (4000, 6000, 8000, 12000)
+    grids = [(nz, nx) for nz, nx, *_ in bench.UNEVEN]
+    assert grids == [(401, 801), (601, 1201), (1001, 2001), (1501, 3001)]
+    assert {fd for _, _, _, fd, _, _ in bench.UNEVEN} == {4, 8}
+    assert all(20 <= npml <= 40 and 60.0 <= fc <= 120.0 for *_, npml, fc in bench.UNEVEN)
+    for k, ((nz, nx, _, fd, npml, fc), nt) in enumerate(zip(bench.UNEVEN, bench.UNEVEN_FULL_NT)):
+        sv, true, _ = S.config_layered(nz=nz, nx=nx, dx=0.5, nt=nt, dt=5e-5, nshot=bench.UNEVEN_SHOTS,
+                                       fdorder=fd, npml=npml, nrec=200, snap_dt=3, fc=fc,
+                                       seed=100 + k, surf_offset=0)
+        assert (sv.nz, sv.nx, sv.nt, sv.fdorder, sv.nshot) == (nz, nx, nt, fd, 32)
+        lam, mu, rho = true
+        out = np.zeros(4)
+        rc = _lib.lib().psv_checkfd_ssg_elastic(sv.nz, sv.nx, sv.dz, sv.dt, sv.freq_pml, npml,
+                                                dptr(rho), dptr(lam), dptr(mu), dptr(sv.hc),
+                                                dptr(out))
+        assert rc == _lib.PSV_OK and sv.dt < out[0], (k, out)
